@@ -1,0 +1,74 @@
+// common.cuh -- shared definitions for the GB300 NFFT kernels and host runtime.
+//
+// Data layout in HBM (per transform instance):
+//   x      [M][d]  float64 nodes (the reference's layout, src/cunfft_typedefs.h:129-131)
+//   f_hat  row-major over I_N, dim 0 slowest (k_t + N_t/2 is the index along dim t)
+//   g      row-major n0 x n1 x n2 oversampled grid; frequency k lives at k mod n
+//   f      [M] samples
+// Batched plans store B instances back to back (B*N_total coefficients, B*n_total
+// grid points, sum_i M_i nodes/samples).  Complex values are interleaved (re, im)
+// pairs of the plan's real type: double2 for the FP64 form, float2 for the FP32 form.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace cg {
+
+constexpr int kMaxDim = 3;
+constexpr int kMaxTaps = 32;        // W = 2m+2 <= 32, i.e. 1 <= m <= 15
+constexpr int kWarp = 32;
+
+template <typename T> struct Cx;
+template <> struct Cx<float>  { using t = float2; };
+template <> struct Cx<double> { using t = double2; };
+
+// Geometry of one plan, passed by value to every kernel.
+struct Geom {
+  int d;                 // 1..3
+  int m;                 // window cut-off
+  int W;                 // taps per dimension, 2m+2
+  int batch;             // number of instances
+  int64_t N[kMaxDim];    // bandwidths (1 for unused dims)
+  int64_t n[kMaxDim];    // oversampled grid sizes, powers of two (1 for unused dims)
+  int64_t Ntot, ntot;    // per instance
+  double b[kMaxDim];     // Gaussian shape parameter per dim
+  double norm;           // prod_t sqrt(b'_t), b' = (2 sigma-1)/(2 sigma m) = 1/(pi b)
+};
+
+// Tiling of the oversampled grid used by the gridding kernels.
+struct Tiling {
+  int T[kMaxDim];        // tile extent per dim (power of two, <= n_t)
+  int nb[kMaxDim];       // tiles per dim = n_t / T_t
+  int E[kMaxDim];        // padded extent per dim = T_t + W - 1
+  int S;                 // shared-memory row stride (elements) for the innermost dim
+  int R1;                // rows per plane (E[d-2] for d = 3, unused otherwise)
+  int64_t tiles_per_inst;
+  int64_t tiles_total;   // batch * tiles_per_inst
+  int chunk;             // max nodes per work item
+  int threads;           // CTA size of the gridding kernels
+  size_t smem_tile;      // bytes of the staged tile
+};
+
+// Sorted node records, produced by the binning kernels.
+struct Bins {
+  int32_t* sidx;         // [M] original node index of the k-th sorted node
+  int32_t* soff;         // [M] packed tile-local window start (10 bits per dim)
+  void*    sfrac;        // [M*d] T: c_t - m with c_t = n_t x_t - u_t (FP64 reduction)
+  int32_t* count;        // [tiles_total + 1]
+  int32_t* tile_off;     // [tiles_total + 1] exclusive scan of counts
+  int32_t* item_off;     // [tiles_total + 1] exclusive scan of items per tile
+  int4*    items;        // [max_items] (tile, start, end, 0)
+  int32_t* num_items;    // [1]
+  int32_t* work;         // [2] persistent work-queue counters (forward, adjoint)
+  int2*    tile_rank;    // [M] per node (tile, rank) scratch
+  int32_t* inst_off;     // [batch + 1] node offsets per instance
+  int32_t* status;       // [1] device-side error flag
+  int64_t  M;            // total nodes
+  int64_t  max_items;
+  int      valid;        // nodes binned for the current tiling
+};
+
+__host__ __device__ inline int64_t wrap_pow2(int64_t i, int64_t n) { return i & (n - 1); }
+
+}  // namespace cg

@@ -1,0 +1,151 @@
+// kernels_bin.cu -- node binning: FP64 node-to-grid reduction and counting sort by tile.
+//
+// For every node and dimension t the window start is the reference's rule
+// (src/cunfft_kernel.cu:175-182)
+//     u_t = llrint(n_t x_t) - signbit(x_t) - m,    c_t = n_t x_t - u_t,
+// and the 2m+2 taps of the node cover grid indices (u_t + l) mod n_t.  The node is
+// filed under the tile that holds its wrapped window start s_t = u_t mod n_t; the
+// tile-local start o_t = s_t mod T_t and the fraction c_t - m (exact in FP64, then
+// rounded to the plan's real type) are what the gridding kernels need.
+#include "runtime.h"
+
+namespace cg {
+
+__device__ __forceinline__ int find_instance(const int32_t* __restrict__ inst_off, int batch, int64_t j) {
+  int lo = 0, hi = batch;  // inst_off[lo] <= j < inst_off[hi]
+  while (hi - lo > 1) {
+    int mid = (lo + hi) >> 1;
+    if (inst_off[mid] <= j) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ void reduce_coord(double x, int64_t n, int m, int64_t& u, double& c) {
+  double nx = __dmul_rn(x, (double)n);
+  u = (int64_t)__double2ll_rn(nx) - (signbit(x) ? 1 : 0) - (int64_t)m;
+  c = __dsub_rn(nx, (double)u);
+}
+
+__global__ void k_bin_count(const double* __restrict__ x, int64_t M, Geom geo, Tiling tl,
+                            const int32_t* __restrict__ inst_off, int32_t* __restrict__ count,
+                            int2* __restrict__ tile_rank) {
+  const int d = geo.d;
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < M; j += (int64_t)gridDim.x * blockDim.x) {
+    int inst = geo.batch > 1 ? find_instance(inst_off, geo.batch, j) : 0;
+    int64_t tile = 0;
+    for (int t = 0; t < d; ++t) {
+      int64_t u; double c;
+      reduce_coord(x[j * d + t], geo.n[t], geo.m, u, c);
+      int64_t s = wrap_pow2(u, geo.n[t]);
+      tile = tile * tl.nb[t] + s / tl.T[t];
+    }
+    tile += (int64_t)inst * tl.tiles_per_inst;
+    int rank = atomicAdd(&count[tile], 1);
+    tile_rank[j] = make_int2((int)tile, rank);
+  }
+}
+
+template <typename T>
+__global__ void k_bin_scatter(const double* __restrict__ x, int64_t M, Geom geo, Tiling tl,
+                              const int2* __restrict__ tile_rank, const int32_t* __restrict__ tile_off,
+                              int32_t* __restrict__ sidx, int32_t* __restrict__ soff, T* __restrict__ sfrac) {
+  const int d = geo.d;
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < M; j += (int64_t)gridDim.x * blockDim.x) {
+    int2 tr = tile_rank[j];
+    int64_t pos = (int64_t)tile_off[tr.x] + tr.y;
+    uint32_t packed = 0;
+    for (int t = 0; t < d; ++t) {
+      int64_t u; double c;
+      reduce_coord(x[j * d + t], geo.n[t], geo.m, u, c);
+      int64_t s = wrap_pow2(u, geo.n[t]);
+      uint32_t o = (uint32_t)(s % tl.T[t]);
+      packed |= o << (10 * t);
+      sfrac[pos * d + t] = (T)(c - (double)geo.m);
+    }
+    sidx[pos] = (int32_t)j;
+    soff[pos] = (int32_t)packed;
+  }
+}
+
+// Single-CTA exclusive scan of the per-tile counts and of the per-tile work-item
+// counts ceil(count / chunk).  Each thread scans a contiguous segment.
+__global__ void __launch_bounds__(1024) k_scan_tiles(const int32_t* __restrict__ count, int64_t ntiles, int chunk,
+                                                     int32_t* __restrict__ tile_off, int32_t* __restrict__ item_off,
+                                                     int32_t* __restrict__ num_items) {
+  __shared__ int64_t sc[1024], si[1024];
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int64_t seg = (ntiles + nt - 1) / nt;
+  const int64_t lo = min(ntiles, tid * seg), hi = min(ntiles, lo + seg);
+  int64_t c = 0, it = 0;
+  for (int64_t i = lo; i < hi; ++i) {
+    int32_t v = count[i];
+    c += v;
+    it += (v + chunk - 1) / chunk;
+  }
+  sc[tid] = c;
+  si[tid] = it;
+  __syncthreads();
+  for (int off = 1; off < nt; off <<= 1) {
+    int64_t a = tid >= off ? sc[tid - off] : 0, b = tid >= off ? si[tid - off] : 0;
+    __syncthreads();
+    sc[tid] += a;
+    si[tid] += b;
+    __syncthreads();
+  }
+  int64_t rc = sc[tid] - c, ri = si[tid] - it;
+  for (int64_t i = lo; i < hi; ++i) {
+    int32_t v = count[i];
+    tile_off[i] = (int32_t)rc;
+    item_off[i] = (int32_t)ri;
+    rc += v;
+    ri += (v + chunk - 1) / chunk;
+  }
+  if (tid == nt - 1) {
+    tile_off[ntiles] = (int32_t)sc[tid];
+    item_off[ntiles] = (int32_t)si[tid];
+    *num_items = (int32_t)si[tid];
+  }
+}
+
+__global__ void k_make_items(const int32_t* __restrict__ count, const int32_t* __restrict__ tile_off,
+                             const int32_t* __restrict__ item_off, int64_t ntiles, int chunk,
+                             int4* __restrict__ items) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < ntiles; t += (int64_t)gridDim.x * blockDim.x) {
+    int32_t c = count[t], s = tile_off[t], io = item_off[t];
+    for (int32_t k = 0; k * chunk < c; ++k) {
+      int32_t a = s + k * chunk;
+      items[io + k] = make_int4((int)t, a, min(s + c, a + chunk), 0);
+    }
+  }
+}
+
+static inline int grid_for(int64_t work, int threads, int sms) {
+  int64_t b = (work + threads - 1) / threads;
+  int64_t cap = (int64_t)sms * 32;
+  if (b > cap) b = cap;
+  return (int)(b < 1 ? 1 : b);
+}
+
+cudaError_t launch_binning(const Plan& p, const double* x, cudaStream_t st) {
+  const Bins& B = p.bins;
+  const Tiling& tl = p.tl;
+  cudaError_t e = cudaMemsetAsync(B.count, 0, sizeof(int32_t) * (tl.tiles_total + 1), st);
+  if (e != cudaSuccess) return e;
+  if (B.M > 0) {
+    k_bin_count<<<grid_for(B.M, 256, p.num_sms), 256, 0, st>>>(x, B.M, p.geo, tl, B.inst_off, B.count, B.tile_rank);
+  }
+  k_scan_tiles<<<1, 1024, 0, st>>>(B.count, tl.tiles_total, tl.chunk, B.tile_off, B.item_off, B.num_items);
+  if (B.M > 0) {
+    if (p.prec == kF64)
+      k_bin_scatter<double><<<grid_for(B.M, 256, p.num_sms), 256, 0, st>>>(
+          x, B.M, p.geo, tl, B.tile_rank, B.tile_off, B.sidx, B.soff, (double*)B.sfrac);
+    else
+      k_bin_scatter<float><<<grid_for(B.M, 256, p.num_sms), 256, 0, st>>>(
+          x, B.M, p.geo, tl, B.tile_rank, B.tile_off, B.sidx, B.soff, (float*)B.sfrac);
+    k_make_items<<<grid_for(tl.tiles_total, 256, p.num_sms), 256, 0, st>>>(B.count, B.tile_off, B.item_off,
+                                                                            tl.tiles_total, tl.chunk, B.items);
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace cg

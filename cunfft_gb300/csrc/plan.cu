@@ -1,0 +1,475 @@
+// plan.cu -- plan life cycle and transform sequencing (host side).
+//
+// Stage order (reference src/cunfft.cu:196-224, src/cunfft_wrapper.cu):
+//   forward:  roll-off + zero-pad  ->  FFT (e^-)  ->  interpolation
+//   adjoint:  clear grid -> spreading ->  FFT (e^+) ->  crop + roll-off
+// All stages are asynchronous on the plan's stream; no stage synchronises.
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "runtime.h"
+
+namespace cg {
+
+int set_status(Plan* p, int code, const char* fmt, ...) {
+  if (p) {
+    p->last_status = code;
+    if (code != CUNFFT_X_SUCCESS && fmt) {
+      va_list ap;
+      va_start(ap, fmt);
+      vsnprintf(p->last_msg, sizeof(p->last_msg), fmt, ap);
+      va_end(ap);
+    } else if (code == CUNFFT_X_SUCCESS) {
+      p->last_msg[0] = 0;
+    }
+  }
+  return code;
+}
+
+int check_cuda(Plan* p, cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return CUNFFT_X_SUCCESS;
+  const int code = e == cudaErrorMemoryAllocation ? CUNFFT_X_ALLOC_FAILED : CUNFFT_X_CUDA_ERROR;
+  return set_status(p, code, "%s: %s", what, cudaGetErrorString(e));
+}
+
+int check_cufft(Plan* p, cufftResult r, const char* what) {
+  if (r == CUFFT_SUCCESS) return CUNFFT_X_SUCCESS;
+  return set_status(p, r == CUFFT_ALLOC_FAILED ? CUNFFT_X_ALLOC_FAILED : CUNFFT_X_CUFFT_ERROR,
+                    "%s: cuFFT error %d", what, (int)r);
+}
+
+#define CG_TRY(expr)                          \
+  do {                                        \
+    int _s = (expr);                          \
+    if (_s != CUNFFT_X_SUCCESS) return _s;    \
+  } while (0)
+
+static bool is_pow2(int64_t v) { return v > 0 && (v & (v - 1)) == 0; }
+
+static size_t elem_bytes(const Plan* p) { return p->prec == kF64 ? 16 : 8; }
+
+static void free_bins(Plan* p) {
+  Bins& B = p->bins;
+  cudaFree(B.sidx);
+  cudaFree(B.soff);
+  cudaFree(B.sfrac);
+  cudaFree(B.tile_rank);
+  cudaFree(B.count);
+  cudaFree(B.tile_off);
+  cudaFree(B.item_off);
+  cudaFree(B.items);
+  B.sidx = nullptr; B.soff = nullptr; B.sfrac = nullptr; B.tile_rank = nullptr;
+  B.count = nullptr; B.tile_off = nullptr; B.item_off = nullptr; B.items = nullptr;
+  p->bins_capacity_M = -1;
+  p->bins_capacity_tiles = -1;
+}
+
+// Default tile extents: the padded tile must fit the 227 KB of shared memory a
+// CTA may use; FP32 tiles of the 3D kernels leave room for two CTAs per SM.
+static void default_tiles(const Plan* p, int* T) {
+  const int d = p->geo.d;
+  if (d == 1) {
+    T[0] = 2048;
+  } else if (d == 2) {
+    T[0] = 32;
+    T[1] = 64;
+  } else if (p->prec == kF32) {
+    T[0] = 8; T[1] = 4; T[2] = 16;
+  } else {
+    T[0] = 4; T[1] = 4; T[2] = 16;
+  }
+}
+
+int plan_choose_tiling(Plan* p, const int* Tin, int chunk) {
+  const int d = p->geo.d, W = p->geo.W;
+  int T[kMaxDim] = {1, 1, 1};
+  default_tiles(p, T);
+  for (int t = 0; t < d; ++t) {
+    if (Tin && Tin[t] > 0) {
+      if (!is_pow2(Tin[t]) || Tin[t] > 1024)
+        return set_status(p, CUNFFT_X_INVALID_ARGUMENT, "tile extent %d is not a power of two <= 1024", Tin[t]);
+      T[t] = Tin[t];
+    }
+    if (T[t] > p->geo.n[t]) T[t] = (int)p->geo.n[t];
+  }
+  Tiling tl{};
+  for (int t = 0; t < kMaxDim; ++t) {
+    tl.T[t] = t < d ? T[t] : 1;
+    tl.nb[t] = t < d ? (int)(p->geo.n[t] / T[t]) : 1;
+    tl.E[t] = t < d ? T[t] + W - 1 : 1;
+  }
+  const int Elast = tl.E[d - 1];
+  if (d == 1) {
+    tl.S = Elast;
+  } else {
+    int S = Elast;
+    while ((S - W) % 16 != 0) ++S;  // S == W (mod 16): conflict-free lane mapping
+    tl.S = S;
+  }
+  tl.R1 = d == 3 ? tl.E[1] : 1;
+  const int64_t rows = d == 3 ? (int64_t)tl.E[0] * tl.E[1] : (d == 2 ? tl.E[0] : 1);
+  tl.smem_tile = (size_t)(rows * tl.S) * elem_bytes(p);
+  tl.smem_tile = (tl.smem_tile + 15) / 16 * 16;
+  tl.tiles_per_inst = (int64_t)tl.nb[0] * tl.nb[1] * tl.nb[2];
+  tl.tiles_total = tl.tiles_per_inst * p->geo.batch;
+  tl.threads = 256;
+  tl.chunk = chunk > 0 ? chunk : (d == 3 ? 1024 : 2048);
+  Tiling old = p->tl;
+  p->tl = tl;
+  if (gridding_smem_bytes(*p) > 227 * 1024) {
+    p->tl = old;
+    return set_status(p, CUNFFT_X_INVALID_ARGUMENT, "tile needs %zu bytes of shared memory (max 227 KB)",
+                      gridding_smem_bytes(*p));
+  }
+  if (tl.tiles_total >= (int64_t)1 << 31) {
+    p->tl = old;
+    return set_status(p, CUNFFT_X_INVALID_ARGUMENT, "too many tiles");
+  }
+  p->bins.valid = 0;
+  return CUNFFT_X_SUCCESS;
+}
+
+int plan_init(Plan* p, int d, const int64_t* N, const int64_t* n, int m, int prec, int batch, cudaStream_t stream,
+              void* lend_grid) {
+  if (d < 1 || d > kMaxDim) return set_status(p, CUNFFT_X_INVALID_ARGUMENT, "d = %d not in 1..3", d);
+  if (m < 1 || 2 * m + 2 > kMaxTaps) return set_status(p, CUNFFT_X_INVALID_ARGUMENT, "m = %d not in 1..15", m);
+  if (prec != kF64 && prec != kF32) return set_status(p, CUNFFT_X_INVALID_ARGUMENT, "unknown precision %d", prec);
+  if (batch < 1) return set_status(p, CUNFFT_X_INVALID_ARGUMENT, "batch = %d < 1", batch);
+  Geom& g = p->geo;
+  g.d = d;
+  g.m = m;
+  g.W = 2 * m + 2;
+  g.batch = batch;
+  g.Ntot = 1;
+  g.ntot = 1;
+  g.norm = 1.0;
+  for (int t = 0; t < kMaxDim; ++t) {
+    g.N[t] = 1;
+    g.n[t] = 1;
+    g.b[t] = 1.0;
+  }
+  for (int t = 0; t < d; ++t) {
+    if (N[t] < 1) return set_status(p, CUNFFT_X_INVALID_ARGUMENT, "N[%d] = %lld < 1", t, (long long)N[t]);
+    int64_t nt = n ? n[t] : 0;
+    if (nt <= 0) {
+      nt = 1;
+      while (nt < N[t]) nt <<= 1;
+      nt *= 2;
+    }
+    if (!is_pow2(nt))
+      return set_status(p, CUNFFT_X_UNSUPPORTED, "n[%d] = %lld is not a power of two", t, (long long)nt);
+    if (nt < N[t]) return set_status(p, CUNFFT_X_INVALID_ARGUMENT, "n[%d] < N[%d]", t, t);
+    g.N[t] = N[t];
+    g.n[t] = nt;
+    const double sigma = (double)nt / (double)N[t];
+    g.b[t] = (2.0 * sigma) / (2.0 * sigma - 1.0) * ((double)m / M_PI);
+    g.norm *= sqrt((2.0 * sigma - 1.0) / (2.0 * sigma * (double)m));
+    g.Ntot *= N[t];
+    g.ntot *= nt;
+  }
+  if (g.ntot * batch >= ((int64_t)1 << 40)) return set_status(p, CUNFFT_X_INVALID_ARGUMENT, "grid too large");
+  p->prec = prec;
+  CG_TRY(check_cuda(p, cudaGetDevice(&p->device), "cudaGetDevice"));
+  CG_TRY(check_cuda(p, cudaDeviceGetAttribute(&p->num_sms, cudaDevAttrMultiProcessorCount, p->device),
+                    "cudaDeviceGetAttribute"));
+  if (stream) {
+    p->stream = stream;
+    p->own_stream = false;
+  } else {
+    CG_TRY(check_cuda(p, cudaStreamCreate(&p->stream), "cudaStreamCreate"));
+    p->own_stream = true;
+  }
+  for (int i = 0; i < 8; ++i) CG_TRY(check_cuda(p, cudaEventCreate(&p->ev[i]), "cudaEventCreate"));
+  p->timing = true;
+  // roll-off factor tables exp(fac_t k_t^2), fac_t = pi^2 b_t / n_t^2 (src/cunfft.cu:87)
+  {
+    std::vector<double> tab;
+    for (int t = 0; t < d; ++t) {
+      const double fac = (M_PI * M_PI * g.b[t]) / (double)(g.n[t] * g.n[t]);
+      for (int64_t c = 0; c < g.N[t]; ++c) {
+        const double k = (double)(c - g.N[t] / 2);
+        tab.push_back(exp(fac * k * k));
+      }
+    }
+    CG_TRY(check_cuda(p, cudaMalloc(&p->roc_tab, sizeof(double) * tab.size()), "cudaMalloc roll-off table"));
+    CG_TRY(check_cuda(p, cudaMemcpy(p->roc_tab, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice),
+                      "upload roll-off table"));
+  }
+  if (lend_grid) {
+    p->g = lend_grid;
+    p->own_g = false;
+  } else {
+    CG_TRY(check_cuda(p, cudaMalloc(&p->g, elem_bytes(p) * g.ntot * batch), "cudaMalloc grid"));
+    p->own_g = true;
+  }
+  // batched in-place FFT over the instances' grids
+  {
+    int nn[kMaxDim];
+    for (int t = 0; t < d; ++t) {
+      if (g.n[t] > 0x7fffffff) return set_status(p, CUNFFT_X_UNSUPPORTED, "FFT length too large");
+      nn[t] = (int)g.n[t];
+    }
+    cufftHandle h;
+    CG_TRY(check_cufft(p, cufftCreate(&h), "cufftCreate"));
+    size_t ws = 0;
+    long long nll[kMaxDim];
+    for (int t = 0; t < d; ++t) nll[t] = nn[t];
+    cufftResult r = cufftMakePlanMany64(h, d, nll, nullptr, 1, g.ntot, nullptr, 1, g.ntot,
+                                        prec == kF64 ? CUFFT_Z2Z : CUFFT_C2C, batch, &ws);
+    if (r != CUFFT_SUCCESS) {
+      cufftDestroy(h);
+      return check_cufft(p, r, "cufftMakePlanMany64");
+    }
+    p->fft = h;
+    p->own_fft = true;
+  }
+  // per-instance node offsets, status flag, work counters
+  CG_TRY(check_cuda(p, cudaMalloc(&p->bins.inst_off, sizeof(int32_t) * (batch + 1)), "cudaMalloc"));
+  CG_TRY(check_cuda(p, cudaMalloc(&p->bins.work, sizeof(int32_t) * 2), "cudaMalloc"));
+  CG_TRY(check_cuda(p, cudaMalloc(&p->bins.num_items, sizeof(int32_t)), "cudaMalloc"));
+  CG_TRY(check_cuda(p, cudaMalloc(&p->bins.status, sizeof(int32_t)), "cudaMalloc"));
+  CG_TRY(check_cuda(p, cudaMemset(p->bins.status, 0, sizeof(int32_t)), "cudaMemset"));
+  p->M_inst = (int64_t*)calloc((size_t)batch, sizeof(int64_t));
+  CG_TRY(plan_choose_tiling(p, nullptr, 0));
+  return set_status(p, CUNFFT_X_SUCCESS, nullptr);
+}
+
+void plan_release(Plan* p) {
+  if (!p) return;
+  if (p->stream) cudaStreamSynchronize(p->stream);
+  free_bins(p);
+  cudaFree(p->bins.inst_off);
+  cudaFree(p->bins.work);
+  cudaFree(p->bins.num_items);
+  cudaFree(p->bins.status);
+  p->bins.inst_off = nullptr;
+  p->bins.work = nullptr;
+  p->bins.num_items = nullptr;
+  p->bins.status = nullptr;
+  if (p->own_g) cudaFree(p->g);
+  p->g = nullptr;
+  cudaFree(p->roc_tab);
+  p->roc_tab = nullptr;
+  if (p->own_fft && p->fft) cufftDestroy(p->fft);
+  p->fft = 0;
+  for (int i = 0; i < 8; ++i)
+    if (p->ev[i]) cudaEventDestroy(p->ev[i]);
+  if (p->own_stream && p->stream) cudaStreamDestroy(p->stream);
+  p->stream = nullptr;
+  free(p->M_inst);
+  p->M_inst = nullptr;
+}
+
+static int ensure_bins(Plan* p, int64_t M) {
+  Bins& B = p->bins;
+  const int64_t tiles = p->tl.tiles_total;
+  const int64_t max_items = tiles + M / std::max(1, p->tl.chunk) + 1;
+  const size_t real = elem_bytes(p) / 2;
+  if (M > p->bins_capacity_M || tiles > p->bins_capacity_tiles || max_items > B.max_items ||
+      p->bins_capacity_M < 0) {
+    const int64_t capM = std::max<int64_t>(M, 1), capT = tiles;
+    free_bins(p);
+    CG_TRY(check_cuda(p, cudaMalloc(&B.sidx, sizeof(int32_t) * capM), "cudaMalloc bins"));
+    CG_TRY(check_cuda(p, cudaMalloc(&B.soff, sizeof(int32_t) * capM), "cudaMalloc bins"));
+    CG_TRY(check_cuda(p, cudaMalloc(&B.sfrac, real * p->geo.d * capM), "cudaMalloc bins"));
+    CG_TRY(check_cuda(p, cudaMalloc(&B.tile_rank, sizeof(int2) * capM), "cudaMalloc bins"));
+    CG_TRY(check_cuda(p, cudaMalloc(&B.count, sizeof(int32_t) * (capT + 1)), "cudaMalloc bins"));
+    CG_TRY(check_cuda(p, cudaMalloc(&B.tile_off, sizeof(int32_t) * (capT + 1)), "cudaMalloc bins"));
+    CG_TRY(check_cuda(p, cudaMalloc(&B.item_off, sizeof(int32_t) * (capT + 1)), "cudaMalloc bins"));
+    const int64_t cap_items = capT + capM / std::max(1, p->tl.chunk) + 1;
+    CG_TRY(check_cuda(p, cudaMalloc(&B.items, sizeof(int4) * cap_items), "cudaMalloc bins"));
+    B.max_items = cap_items;
+    p->bins_capacity_M = capM;
+    p->bins_capacity_tiles = capT;
+  }
+  return CUNFFT_X_SUCCESS;
+}
+
+static int rebin(Plan* p) {
+  CG_TRY(ensure_bins(p, p->M));
+  p->bins.M = p->M;
+  if (p->timing) cudaEventRecord(p->ev[6], p->stream);
+  CG_TRY(check_cuda(p, launch_binning(*p, p->x, p->stream), "binning kernels"));
+  if (p->timing) cudaEventRecord(p->ev[7], p->stream);
+  p->bins.valid = 1;
+  return CUNFFT_X_SUCCESS;
+}
+
+int plan_set_nodes(Plan* p, const double* x, const int64_t* M_inst) {
+  int64_t M = 0;
+  std::vector<int32_t> off((size_t)p->geo.batch + 1, 0);
+  for (int i = 0; i < p->geo.batch; ++i) {
+    if (M_inst[i] < 0) return set_status(p, CUNFFT_X_INVALID_ARGUMENT, "M[%d] < 0", i);
+    M += M_inst[i];
+    if (M >= ((int64_t)1 << 31) - 1) return set_status(p, CUNFFT_X_UNSUPPORTED, "more than 2^31-2 nodes");
+    off[i + 1] = (int32_t)M;
+    p->M_inst[i] = M_inst[i];
+  }
+  if (M > 0 && !x) return set_status(p, CUNFFT_X_INVALID_ARGUMENT, "x is NULL");
+  CG_TRY(check_cuda(p, cudaMemcpyAsync(p->bins.inst_off, off.data(), sizeof(int32_t) * off.size(),
+                                       cudaMemcpyHostToDevice, p->stream), "upload node offsets"));
+  // the host vector must outlive the async copy
+  CG_TRY(check_cuda(p, cudaStreamSynchronize(p->stream), "cudaStreamSynchronize"));
+  p->x = x;
+  p->M = M;
+  CG_TRY(rebin(p));
+  p->nodes_set = true;
+  p->t_bin = 0;
+  return set_status(p, CUNFFT_X_SUCCESS, nullptr);
+}
+
+static cufftResult exec_fft(const Plan* p, cufftHandle h, void* data, int dir) {
+  cufftResult r = cufftSetStream(h, p->stream);
+  if (r != CUFFT_SUCCESS) return r;
+  if (p->prec == kF64) return cufftExecZ2Z(h, (cufftDoubleComplex*)data, (cufftDoubleComplex*)data, dir);
+  return cufftExecC2C(h, (cufftComplex*)data, (cufftComplex*)data, dir);
+}
+
+static void rec(Plan* p, int i) {
+  if (p->timing) cudaEventRecord(p->ev[i], p->stream);
+}
+
+int plan_forward(Plan* p, const void* fhat, void* f) {
+  if (!p->nodes_set) return set_status(p, CUNFFT_X_NODES_NOT_SET, "forward: nodes not set");
+  if (!p->bins.valid) CG_TRY(rebin(p));
+  rec(p, 0);
+  CG_TRY(check_cuda(p, launch_roc_forward(*p, fhat, p->g, p->stream), "roll-off kernel"));
+  rec(p, 1);
+  CG_TRY(check_cufft(p, exec_fft(p, p->fft_fwd_ext ? p->fft_fwd_ext : p->fft, p->g, CUFFT_FORWARD), "forward FFT"));
+  rec(p, 2);
+  CG_TRY(check_cuda(p, launch_interp(*p, p->g, f, p->stream), "interpolation kernel"));
+  rec(p, 3);
+  return set_status(p, CUNFFT_X_SUCCESS, nullptr);
+}
+
+int plan_adjoint(Plan* p, const void* f, void* fhat) {
+  if (!p->nodes_set) return set_status(p, CUNFFT_X_NODES_NOT_SET, "adjoint: nodes not set");
+  if (!p->bins.valid) CG_TRY(rebin(p));
+  rec(p, 0);
+  CG_TRY(check_cuda(p, cudaMemsetAsync(p->g, 0, elem_bytes(p) * p->geo.ntot * p->geo.batch, p->stream),
+                    "clear grid"));
+  CG_TRY(check_cuda(p, launch_spread(*p, f, p->g, p->stream), "spreading kernel"));
+  rec(p, 1);
+  CG_TRY(check_cufft(p, exec_fft(p, p->fft_bwd_ext ? p->fft_bwd_ext : p->fft, p->g, CUFFT_INVERSE), "adjoint FFT"));
+  rec(p, 2);
+  CG_TRY(check_cuda(p, launch_roc_adjoint(*p, p->g, fhat, p->stream), "roll-off kernel"));
+  rec(p, 3);
+  return set_status(p, CUNFFT_X_SUCCESS, nullptr);
+}
+
+int plan_interp_only(Plan* p, const void* g, void* f) {
+  if (!p->nodes_set) return set_status(p, CUNFFT_X_NODES_NOT_SET, "interp: nodes not set");
+  if (!p->bins.valid) CG_TRY(rebin(p));
+  CG_TRY(check_cuda(p, launch_interp(*p, g, f, p->stream), "interpolation kernel"));
+  return set_status(p, CUNFFT_X_SUCCESS, nullptr);
+}
+
+int plan_spread_only(Plan* p, const void* f, void* g) {
+  if (!p->nodes_set) return set_status(p, CUNFFT_X_NODES_NOT_SET, "spread: nodes not set");
+  if (!p->bins.valid) CG_TRY(rebin(p));
+  CG_TRY(check_cuda(p, launch_spread(*p, f, g, p->stream), "spreading kernel"));
+  return set_status(p, CUNFFT_X_SUCCESS, nullptr);
+}
+
+int plan_ndft_forward(Plan* p, const void* fhat, void* f) {
+  if (!p->nodes_set) return set_status(p, CUNFFT_X_NODES_NOT_SET, "ndft: nodes not set");
+  CG_TRY(check_cuda(p, launch_ndft_forward(*p, p->x, fhat, f, p->stream), "NDFT kernel"));
+  return set_status(p, CUNFFT_X_SUCCESS, nullptr);
+}
+
+int plan_ndft_adjoint(Plan* p, const void* f, void* fhat, const int64_t* kidx, int64_t nsel) {
+  if (!p->nodes_set) return set_status(p, CUNFFT_X_NODES_NOT_SET, "ndft: nodes not set");
+  if (kidx && nsel < 0) return set_status(p, CUNFFT_X_INVALID_ARGUMENT, "nsel < 0");
+  CG_TRY(check_cuda(p, launch_ndft_adjoint(*p, p->x, f, fhat, p->stream, kidx, nsel), "adjoint NDFT kernel"));
+  return set_status(p, CUNFFT_X_SUCCESS, nullptr);
+}
+
+int plan_node_gradient(Plan* p, const void* fhat, const void* grad_f, double* grad_x) {
+  if (!p->nodes_set) return set_status(p, CUNFFT_X_NODES_NOT_SET, "gradient: nodes not set");
+  CG_TRY(check_cuda(p, launch_roc_forward(*p, fhat, p->g, p->stream), "roll-off kernel"));
+  CG_TRY(check_cufft(p, exec_fft(p, p->fft, p->g, CUFFT_FORWARD), "forward FFT"));
+  CG_TRY(check_cuda(p, launch_interp_grad(*p, p->g, grad_f, grad_x, p->stream), "gradient kernel"));
+  return set_status(p, CUNFFT_X_SUCCESS, nullptr);
+}
+
+// Autotuner: time interpolation and spreading for a few tilings on the bound
+// node set; keep the tiling with the smallest sum.  Restores the previous tiling
+// when a candidate fails.
+int plan_autotune(Plan* p, int reps) {
+  if (!p->nodes_set) return set_status(p, CUNFFT_X_NODES_NOT_SET, "autotune: nodes not set");
+  if (reps < 1) reps = 1;
+  const int d = p->geo.d;
+  std::vector<std::vector<int>> cands;
+  if (d == 1) {
+    for (int t : {512, 1024, 2048, 4096, 8192}) cands.push_back({t, 1, 1});
+  } else if (d == 2) {
+    for (int a : {16, 32, 64})
+      for (int b : {32, 64, 128}) cands.push_back({a, b, 1});
+  } else if (p->prec == kF32) {
+    cands = {{8, 4, 16}, {4, 8, 16}, {8, 8, 16}, {16, 16, 16}, {8, 16, 16}, {4, 4, 32}, {8, 4, 32}};
+  } else {
+    cands = {{4, 4, 16}, {8, 4, 16}, {4, 8, 16}, {4, 4, 32}, {8, 8, 8}};
+  }
+  const Tiling best0 = p->tl;
+  float best = 3.0e38f;
+  std::vector<int> best_T(3, 0);
+  const size_t bytes = elem_bytes(p);
+  void* scratch_f = nullptr;
+  if (check_cuda(p, cudaMalloc(&scratch_f, bytes * std::max<int64_t>(p->M, 1)), "autotune scratch")) return p->last_status;
+  // non-zero data so that the spreading flush does real work while timed
+  cudaMemsetAsync(scratch_f, 0x3c, bytes * std::max<int64_t>(p->M, 1), p->stream);
+  cudaMemsetAsync(p->g, 0x3c, bytes * p->geo.ntot * p->geo.batch, p->stream);
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  const bool timing = p->timing;
+  p->timing = false;
+  for (auto& c : cands) {
+    int T[3] = {c[0], c[1], c[2]};
+    bool fits = true;
+    for (int t = 0; t < d; ++t) fits = fits && T[t] <= p->geo.n[t];
+    if (!fits) continue;
+    if (plan_choose_tiling(p, T, p->chunk_override) != CUNFFT_X_SUCCESS) continue;
+    if (rebin(p) != CUNFFT_X_SUCCESS) break;
+    // warm-up
+    if (launch_interp(*p, p->g, scratch_f, p->stream) != cudaSuccess) continue;
+    if (launch_spread(*p, scratch_f, p->g, p->stream) != cudaSuccess) continue;
+    cudaEventRecord(a, p->stream);
+    for (int r = 0; r < reps; ++r) {
+      launch_interp(*p, p->g, scratch_f, p->stream);
+      launch_spread(*p, scratch_f, p->g, p->stream);
+    }
+    cudaEventRecord(b, p->stream);
+    if (cudaEventSynchronize(b) != cudaSuccess) break;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    if (ms < best) {
+      best = ms;
+      best_T = {T[0], T[1], T[2]};
+    }
+  }
+  p->timing = timing;
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(scratch_f);
+  cudaGetLastError();
+  if (best_T[0] == 0) {
+    p->tl = best0;
+    p->bins.valid = 0;
+    return set_status(p, CUNFFT_X_CUDA_ERROR, "autotune: no candidate ran");
+  }
+  int T[3] = {best_T[0], best_T[1], best_T[2]};
+  CG_TRY(plan_choose_tiling(p, T, p->chunk_override));
+  CG_TRY(rebin(p));
+  // the grid holds garbage from the timing runs; transforms rewrite it fully
+  p->autotuned = true;
+  return set_status(p, CUNFFT_X_SUCCESS, nullptr);
+}
+
+}  // namespace cg

@@ -1,0 +1,88 @@
+// runtime.h -- host runtime of the GB300 NFFT: plan object, launchers, status codes.
+//
+// One Plan describes B transform instances that share d, N, n and m.  It owns the
+// oversampled grid (unless the caller lends one, as the drop-in ABI does with
+// cunfft_plan::g_gpu), the cuFFT plan, the binning buffers and a CUDA stream.
+// Every kernel argument is passed by value: there is no global __constant__
+// state, so any number of plans coexist and run concurrently on their streams.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cufft.h>
+#include <stdint.h>
+
+#include "common.cuh"
+#include "cunfft_x.h"
+
+namespace cg {
+
+enum Precision { kF64 = CUNFFT_X_F64, kF32 = CUNFFT_X_F32 };
+
+struct Plan {
+  Geom geo{};
+  int prec = kF64;
+  int num_sms = 0;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  cufftHandle fft = 0;         // batched plan used for both directions
+  bool own_fft = false;
+  cufftHandle fft_fwd_ext = 0; // handles lent by the drop-in ABI (0: use fft)
+  cufftHandle fft_bwd_ext = 0;
+  void* g = nullptr;           // batch * ntot complex
+  bool own_g = false;
+  double* roc_tab = nullptr;   // per-dim roll-off factors exp(fac_t k_t^2), sum_t N_t doubles
+  Tiling tl{};
+  Bins bins{};
+  int64_t bins_capacity_M = -1;
+  int64_t bins_capacity_tiles = -1;
+  const double* x = nullptr;   // device nodes of the current node set
+  int64_t M = 0;
+  int64_t* M_inst = nullptr;   // host copy of per-instance node counts
+  bool nodes_set = false;
+  int tile_override[kMaxDim] = {0, 0, 0};
+  int chunk_override = 0;
+  bool autotuned = false;
+  int last_status = 0;
+  char last_msg[256] = {0};
+  // per-stage timing of the last call (seconds), recorded with events on the plan stream
+  cudaEvent_t ev[8] = {};
+  bool timing = false;
+  double t_bin = 0, t_roc = 0, t_fft = 0, t_conv = 0;
+};
+
+// status helpers
+int set_status(Plan* p, int code, const char* fmt, ...);
+int check_cuda(Plan* p, cudaError_t e, const char* what);
+int check_cufft(Plan* p, cufftResult r, const char* what);
+
+// plan life cycle (plan.cu)
+int plan_init(Plan* p, int d, const int64_t* N, const int64_t* n, int m, int prec, int batch,
+              cudaStream_t stream, void* lend_grid);
+void plan_release(Plan* p);
+int plan_set_nodes(Plan* p, const double* x, const int64_t* M_inst);
+int plan_forward(Plan* p, const void* fhat, void* f);
+int plan_adjoint(Plan* p, const void* f, void* fhat);
+int plan_interp_only(Plan* p, const void* g, void* f);
+int plan_spread_only(Plan* p, const void* f, void* g);
+int plan_ndft_forward(Plan* p, const void* fhat, void* f);
+int plan_ndft_adjoint(Plan* p, const void* f, void* fhat, const int64_t* kidx = nullptr, int64_t nsel = 0);
+int plan_node_gradient(Plan* p, const void* fhat, const void* grad_f, double* grad_x);
+int plan_choose_tiling(Plan* p, const int* T, int chunk);
+int plan_autotune(Plan* p, int reps);
+
+// launchers (kernel .cu files); all asynchronous on st
+cudaError_t launch_binning(const Plan& p, const double* x, cudaStream_t st);
+cudaError_t launch_roc_forward(const Plan& p, const void* fhat, void* g, cudaStream_t st);
+cudaError_t launch_roc_adjoint(const Plan& p, const void* g, void* fhat, cudaStream_t st);
+cudaError_t launch_interp(const Plan& p, const void* g, void* f, cudaStream_t st);
+cudaError_t launch_spread(const Plan& p, const void* f, void* g, cudaStream_t st);
+cudaError_t launch_interp_grad(const Plan& p, const void* g, const void* grad_f, double* grad_x, cudaStream_t st);
+cudaError_t launch_ndft_forward(const Plan& p, const double* x, const void* fhat, void* f, cudaStream_t st);
+cudaError_t launch_ndft_adjoint(const Plan& p, const double* x, const void* f, void* fhat, cudaStream_t st,
+                                const int64_t* kidx = nullptr, int64_t nsel = 0);
+size_t gridding_smem_bytes(const Plan& p);
+int gridding_max_smem(const Plan& p);
+bool gridding_supported(int d, int W);
+
+}  // namespace cg

@@ -1,0 +1,208 @@
+"""Python front end of the extension API (include/cunfft_x.h) for torch CUDA tensors.
+
+``NFFT`` wraps one cunfft_x plan: d-variate Gaussian-window NFFT (d = 1..3) in
+FP64 (the reference's form) or FP32 (FP32 gridding and FFT, FP64 node
+reduction and roll-off factors), for ``batch`` instances with uneven node
+counts.  Tensors stay on the device; calls run on the plan's CUDA stream, which
+defaults to torch's current stream so they order with surrounding torch work.
+
+Layouts (as the reference): nodes ``x`` float64 (M, d) in [-0.5, 0.5);
+coefficients (batch, *N) row-major with frequency k_t at index k_t + N_t//2;
+samples (M,).
+"""
+import ctypes
+
+import torch
+
+from . import _native as nat
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None and t.numel() > 0 else ctypes.c_void_p(0)
+
+
+class NFFT:
+    def __init__(self, N, n=None, m=6, precision="f64", batch=1, device=None, stream=None):
+        self._lib = nat.lib()
+        self.N = [int(v) for v in N]
+        self.d = len(self.N)
+        if not 1 <= self.d <= 3:
+            raise ValueError("d must be 1, 2 or 3")
+        self.m = int(m)
+        self.batch = int(batch)
+        self.precision = {"f64": nat.F64, "f32": nat.F32, "float64": nat.F64, "float32": nat.F32}[precision]
+        self.cdtype = torch.complex128 if self.precision == nat.F64 else torch.complex64
+        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        with torch.cuda.device(self.device):
+            if stream is None:
+                stream = torch.cuda.current_stream(self.device)
+            self.stream = stream
+            Na = (ctypes.c_int64 * self.d)(*self.N)
+            na = (ctypes.c_int64 * self.d)(*(n if n is not None else [0] * self.d))
+            h = ctypes.c_void_p()
+            st = self._lib.cunfft_x_plan_create(ctypes.byref(h), self.d, Na, na, self.m, self.precision,
+                                                self.batch, ctypes.c_void_p(stream.cuda_stream))
+            nat.check(st)
+        self._h = h
+        self.n = self._grid_sizes(n)
+        self.N_total = 1
+        for v in self.N:
+            self.N_total *= v
+        self.x = None
+        self.M_inst = [0] * self.batch
+        self.M = 0
+
+    def _grid_sizes(self, n):
+        if n is not None:
+            return [int(v) for v in n]
+        out = []
+        for v in self.N:
+            p = 1
+            while p < v:
+                p <<= 1
+            out.append(2 * p)
+        return out
+
+    # ------------------------------------------------------------------ nodes
+    def set_nodes(self, x, M_inst=None):
+        """Bind nodes: x float64 CUDA tensor (sum M_i, d); M_inst per-instance counts."""
+        if x.dtype != torch.float64 or not x.is_cuda:
+            raise TypeError("nodes must be a float64 CUDA tensor")
+        x = x.contiguous().reshape(-1, self.d)
+        M = x.shape[0]
+        if M_inst is None:
+            if self.batch != 1:
+                raise ValueError("M_inst is required for batched plans")
+            M_inst = [M]
+        M_inst = [int(v) for v in M_inst]
+        if len(M_inst) != self.batch or sum(M_inst) != M:
+            raise ValueError("M_inst must have one count per instance summing to x.shape[0]")
+        arr = (ctypes.c_int64 * self.batch)(*M_inst)
+        nat.check(self._lib.cunfft_x_set_nodes(self._h, _ptr(x), arr), self._h)
+        self.x = x  # keep the storage alive: the plan reads it
+        self.M_inst = M_inst
+        self.M = M
+        return self
+
+    # ------------------------------------------------------------ transforms
+    def _coef(self, fhat):
+        fhat = fhat.to(self.cdtype).contiguous()
+        if fhat.numel() != self.batch * self.N_total:
+            raise ValueError("f_hat has the wrong size")
+        return fhat
+
+    def _samples(self, f):
+        f = f.to(self.cdtype).contiguous()
+        if f.numel() != self.M:
+            raise ValueError("f has the wrong size")
+        return f
+
+    def _coef_shape(self):
+        return ([self.batch] if self.batch > 1 else []) + self.N
+
+    def forward(self, fhat, out=None):
+        fhat = self._coef(fhat)
+        f = out if out is not None else torch.empty(self.M, dtype=self.cdtype, device=self.device)
+        nat.check(self._lib.cunfft_x_forward(self._h, _ptr(fhat), _ptr(f)), self._h)
+        return f
+
+    def adjoint(self, f, out=None):
+        f = self._samples(f)
+        fh = out if out is not None else torch.empty(self._coef_shape(), dtype=self.cdtype, device=self.device)
+        nat.check(self._lib.cunfft_x_adjoint(self._h, _ptr(f), _ptr(fh)), self._h)
+        return fh
+
+    def ndft_forward(self, fhat):
+        fhat = fhat.to(torch.complex128).contiguous()
+        f = torch.empty(self.M, dtype=torch.complex128, device=self.device)
+        nat.check(self._lib.cunfft_x_ndft_forward(self._h, _ptr(fhat), _ptr(f)), self._h)
+        return f
+
+    def ndft_adjoint(self, f):
+        f = f.to(torch.complex128).contiguous()
+        fh = torch.empty(self._coef_shape(), dtype=torch.complex128, device=self.device)
+        nat.check(self._lib.cunfft_x_ndft_adjoint(self._h, _ptr(f), _ptr(fh)), self._h)
+        return fh
+
+    def ndft_adjoint_at(self, f, kidx):
+        """Adjoint NDFT at the row-major coefficient indices kidx (int64 CUDA tensor)."""
+        f = f.to(torch.complex128).contiguous()
+        kidx = kidx.to(device=self.device, dtype=torch.int64).contiguous()
+        out = torch.empty(self.batch * kidx.numel(), dtype=torch.complex128, device=self.device)
+        nat.check(self._lib.cunfft_x_ndft_adjoint_at(self._h, _ptr(f), _ptr(kidx), kidx.numel(), _ptr(out)),
+                  self._h)
+        return out
+
+    def node_gradient(self, fhat, grad_f):
+        fhat = self._coef(fhat)
+        grad_f = self._samples(grad_f)
+        gx = torch.empty(self.M, self.d, dtype=torch.float64, device=self.device)
+        nat.check(self._lib.cunfft_x_node_gradient(self._h, _ptr(fhat), _ptr(grad_f), _ptr(gx)), self._h)
+        return gx
+
+    def interp(self, g, out=None):
+        g = g.to(self.cdtype).contiguous()
+        f = out if out is not None else torch.empty(self.M, dtype=self.cdtype, device=self.device)
+        nat.check(self._lib.cunfft_x_interp(self._h, _ptr(g), _ptr(f)), self._h)
+        return f
+
+    def spread(self, f, g=None):
+        f = self._samples(f)
+        if g is None:
+            g = torch.zeros(([self.batch] if self.batch > 1 else []) + self.n, dtype=self.cdtype, device=self.device)
+        nat.check(self._lib.cunfft_x_spread(self._h, _ptr(f), _ptr(g)), self._h)
+        return g
+
+    # ---------------------------------------------------------------- tuning
+    def set_tiling(self, T=None, chunk=0):
+        arr = (ctypes.c_int * 3)(*((list(T) + [0, 0, 0])[:3] if T else [0, 0, 0]))
+        nat.check(self._lib.cunfft_x_set_tiling(self._h, arr, int(chunk)), self._h)
+
+    def tiling(self):
+        T = (ctypes.c_int * 3)()
+        chunk, threads = ctypes.c_int(), ctypes.c_int()
+        nat.check(self._lib.cunfft_x_get_tiling(self._h, T, ctypes.byref(chunk), ctypes.byref(threads)))
+        return {"T": list(T)[: self.d], "chunk": chunk.value, "threads": threads.value}
+
+    def autotune(self, reps=3):
+        nat.check(self._lib.cunfft_x_autotune(self._h, int(reps)), self._h)
+        return self.tiling()
+
+    def stage_times(self):
+        v = [ctypes.c_double() for _ in range(4)]
+        nat.check(self._lib.cunfft_x_stage_times(self._h, *[ctypes.byref(a) for a in v]), self._h)
+        return dict(zip(("bin", "roc", "fft", "conv"), (a.value for a in v)))
+
+    def synchronize(self):
+        nat.check(self._lib.cunfft_x_synchronize(self._h), self._h)
+
+    def grid(self):
+        """The plan's oversampled grid as a tensor view (batch, *n)."""
+        ptr = self._lib.cunfft_x_grid(self._h)
+        numel = self.batch
+        for v in self.n:
+            numel *= v
+        return _wrap_device_pointer(ptr, numel, self.cdtype, self.device).reshape(
+            ([self.batch] if self.batch > 1 else []) + self.n)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.cunfft_x_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _wrap_device_pointer(ptr, numel, dtype, device):
+    """A tensor that aliases device memory owned by the library (no copy)."""
+    class _CudaArray:
+        def __init__(self, p, nbytes):
+            self.__cuda_array_interface__ = {"shape": (nbytes,), "typestr": "|u1", "data": (p, False),
+                                             "version": 3}
+    itemsize = torch.empty((), dtype=dtype).element_size()
+    raw = torch.as_tensor(_CudaArray(ptr, numel * itemsize), device=device)
+    return raw.view(dtype)

@@ -1,0 +1,131 @@
+/*
+ * cunfft_x.h -- extension API of the GB300 NFFT library (libcunfft.so).
+ *
+ * New surface beside the drop-in plan API of cunfft.h.  The reference has no
+ * counterpart for these entry points except where noted: its plan parameters
+ * (m, precision, index width) are compile-time options (src/config.h.in), it
+ * runs one transform per plan on the default stream, and its functions return
+ * void (src/cunfft.h).  Here:
+ *   - m, n and the precision are runtime plan parameters;
+ *   - a plan holds B >= 1 instances with uneven node counts M_i (batched form);
+ *   - all data pointers are DEVICE pointers (float64 nodes, complex data of the
+ *     plan's precision: interleaved double pairs for CUNFFT_X_F64, float pairs
+ *     for CUNFFT_X_F32), and every call is asynchronous on the plan's stream;
+ *   - every entry point returns a cunfft_x_status code and never exits.
+ * Plain C ABI: pointers, sizes and plain integers only.
+ */
+#ifndef CUNFFT_X_H_
+#define CUNFFT_X_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/** Precision of the gridding and FFT stages.  FP64 is the reference's form;
+ *  FP32 keeps FP64 only for the node-to-grid reduction and the roll-off factors. */
+enum { CUNFFT_X_F64 = 0, CUNFFT_X_F32 = 1 };
+
+/** Status codes returned by every cunfft_x_* entry point. */
+enum cunfft_x_status {
+  CUNFFT_X_SUCCESS = 0,
+  CUNFFT_X_INVALID_ARGUMENT = 1,
+  CUNFFT_X_ALLOC_FAILED = 2,
+  CUNFFT_X_CUFFT_ERROR = 3,
+  CUNFFT_X_CUDA_ERROR = 4,
+  CUNFFT_X_NODES_NOT_SET = 5,
+  CUNFFT_X_UNSUPPORTED = 6,
+  CUNFFT_X_DEVICE_CHECK_FAILED = 7
+};
+
+typedef struct cunfft_x_plan cunfft_x_plan;
+
+/** Create a plan.  d in 1..3; N[d] bandwidths; n[d] oversampled grid sizes
+ *  (powers of two with n_t >= N_t; NULL selects n_t = 2*next_pow2(N_t) like
+ *  cunfft_init, src/cunfft.cu:296-299); 1 <= m <= 15; precision CUNFFT_X_F64 or
+ *  CUNFFT_X_F32; batch >= 1 instances; stream 0 creates a private stream
+ *  (a cudaStream_t may be passed as void*). */
+int cunfft_x_plan_create(cunfft_x_plan **plan, int d, const int64_t *N, const int64_t *n, int m,
+                         int precision, int batch, void *stream);
+
+/** Release a plan and its device memory (does not reset the device). */
+int cunfft_x_plan_destroy(cunfft_x_plan *plan);
+
+/** Bind a node set: x is a device array of sum_i M_i * d doubles (instance 0's
+ *  nodes first, each node's d coordinates contiguous), M_inst a HOST array of
+ *  batch node counts.  Bins and sorts the nodes on the device (asynchronous).
+ *  The plan keeps the pointer: x must stay valid until the next set_nodes. */
+int cunfft_x_set_nodes(cunfft_x_plan *plan, const double *x, const int64_t *M_inst);
+
+/** f = A f_hat for every instance: f_hat has batch*N_total complex values,
+ *  f has sum_i M_i (device pointers, plan precision). */
+int cunfft_x_forward(cunfft_x_plan *plan, const void *f_hat, void *f);
+
+/** f_hat = A^H f for every instance. */
+int cunfft_x_adjoint(cunfft_x_plan *plan, const void *f, void *f_hat);
+
+/** Direct NDFT and adjoint NDFT on the bound nodes, always in FP64 with
+ *  complex128 buffers, whatever the plan precision (the error yardstick). */
+int cunfft_x_ndft_forward(cunfft_x_plan *plan, const void *f_hat, void *f);
+int cunfft_x_ndft_adjoint(cunfft_x_plan *plan, const void *f, void *f_hat);
+
+/** Adjoint NDFT at nsel selected coefficients: kidx is a DEVICE array of
+ *  row-major coefficient indices (0 <= kidx < N_total); out receives
+ *  batch*nsel complex128 values (instance-major).  For error checks on large
+ *  plans where the full adjoint NDFT is out of reach. */
+int cunfft_x_ndft_adjoint_at(cunfft_x_plan *plan, const void *f, const int64_t *kidx, int64_t nsel, void *out);
+
+/** Gradient with respect to the node positions of L = sum_j <grad_f_j, f_j>
+ *  where f = A(x) f_hat: grad_x[j*d+t] = Re(conj(grad_f_j) * d f_j / d x_{j,t}),
+ *  evaluated with the derivative of the Gaussian window on the same grid as the
+ *  forward transform.  grad_x is a device array of sum_i M_i * d doubles. */
+int cunfft_x_node_gradient(cunfft_x_plan *plan, const void *f_hat, const void *grad_f, double *grad_x);
+
+/** Gridding stages alone, on a caller-provided oversampled grid g
+ *  (batch*n_total complex, plan precision): interpolation g -> f and
+ *  spreading f -> g (spreading accumulates into g; clear it first). */
+int cunfft_x_interp(cunfft_x_plan *plan, const void *g, void *f);
+int cunfft_x_spread(cunfft_x_plan *plan, const void *f, void *g);
+
+/** Stream used by the plan (cudaStream_t as void*). */
+int cunfft_x_set_stream(cunfft_x_plan *plan, void *stream);
+void *cunfft_x_get_stream(const cunfft_x_plan *plan);
+
+/** Tiling of the gridding kernels: tile extents T[d] (powers of two, each
+ *  <= n_t) and the maximum number of nodes per work item.  Zeros keep the
+ *  defaults.  Re-bins the current node set. */
+int cunfft_x_set_tiling(cunfft_x_plan *plan, const int *T, int chunk);
+
+/** Time the candidate tilings on the bound node set and keep the fastest for
+ *  spreading and interpolation (reps timed calls per candidate). */
+int cunfft_x_autotune(cunfft_x_plan *plan, int reps);
+
+/** Current tiling: T[3], chunk, threads (any pointer may be NULL). */
+int cunfft_x_get_tiling(const cunfft_x_plan *plan, int *T, int *chunk, int *threads);
+
+/** Per-stage device times of the last forward/adjoint call, in seconds
+ *  (binning, roll-off, FFT, gridding).  Blocks until the plan stream is idle. */
+int cunfft_x_stage_times(cunfft_x_plan *plan, double *t_bin, double *t_roc, double *t_fft, double *t_conv);
+
+/** Block until the plan's stream is idle; reports asynchronous errors. */
+int cunfft_x_synchronize(cunfft_x_plan *plan);
+
+/** Last error message of a plan (empty string when none). */
+const char *cunfft_x_last_message(const cunfft_x_plan *plan);
+
+/** Human-readable name of a status code. */
+const char *cunfft_x_status_string(int status);
+
+/** Oversampled grid of the plan (device pointer; valid until destroy). */
+void *cunfft_x_grid(const cunfft_x_plan *plan);
+
+/** Library version string. */
+const char *cunfft_x_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CUNFFT_X_H_ */

@@ -330,39 +330,40 @@ void orc_interp(int d, const int64_t *N, const int64_t *n, int m, int64_t M,
     const int W = p.W;
 #pragma omp parallel for schedule(dynamic, 64)
     for (int64_t j = 0; j < M; ++j) {
-        int64_t u[ORC_MAXD];
+        int64_t u[ORC_MAXD], ix[ORC_MAXD][64];
         double w[ORC_MAXD][64];
         node_setup(&p, x + j * d, u, w);
+        for (int t = 0; t < d; ++t)
+            for (int l = 0; l < W; ++l) ix[t][l] = wrap(u[t] + l, p.n[t]);
         double sr = 0.0, si = 0.0;
         if (d == 1) {
             for (int l0 = 0; l0 < W; ++l0) {
-                int64_t i0 = wrap(u[0] + l0, p.n[0]);
-                sr += g[2 * i0] * w[0][l0];
-                si += g[2 * i0 + 1] * w[0][l0];
+                const double *gp = g + 2 * ix[0][l0];
+                sr += gp[0] * w[0][l0];
+                si += gp[1] * w[0][l0];
             }
         } else if (d == 2) {
             for (int l0 = 0; l0 < W; ++l0) {
-                int64_t i0 = wrap(u[0] + l0, p.n[0]);
+                const double *row = g + 2 * ix[0][l0] * p.n[1];
                 double ar = 0.0, ai = 0.0;
                 for (int l1 = 0; l1 < W; ++l1) {
-                    int64_t gi = i0 * p.n[1] + wrap(u[1] + l1, p.n[1]);
-                    ar += g[2 * gi] * w[1][l1];
-                    ai += g[2 * gi + 1] * w[1][l1];
+                    const double *gp = row + 2 * ix[1][l1];
+                    ar += gp[0] * w[1][l1];
+                    ai += gp[1] * w[1][l1];
                 }
                 sr += ar * w[0][l0];
                 si += ai * w[0][l0];
             }
         } else {
             for (int l0 = 0; l0 < W; ++l0) {
-                int64_t i0 = wrap(u[0] + l0, p.n[0]);
                 double ar = 0.0, ai = 0.0;
                 for (int l1 = 0; l1 < W; ++l1) {
-                    int64_t i1 = wrap(u[1] + l1, p.n[1]);
+                    const double *row = g + 2 * (ix[0][l0] * p.n[1] + ix[1][l1]) * p.n[2];
                     double br = 0.0, bi = 0.0;
                     for (int l2 = 0; l2 < W; ++l2) {
-                        int64_t gi = (i0 * p.n[1] + i1) * p.n[2] + wrap(u[2] + l2, p.n[2]);
-                        br += g[2 * gi] * w[2][l2];
-                        bi += g[2 * gi + 1] * w[2][l2];
+                        const double *gp = row + 2 * ix[2][l2];
+                        br += gp[0] * w[2][l2];
+                        bi += gp[1] * w[2][l2];
                     }
                     ar += br * w[1][l1];
                     ai += bi * w[1][l1];
@@ -378,34 +379,36 @@ void orc_interp(int d, const int64_t *N, const int64_t *n, int m, int64_t M,
 
 static void spread_node(const oplan *p, const double *xj, const double *fj, double *g)
 {
-    int64_t u[ORC_MAXD];
+    int64_t u[ORC_MAXD], ix[ORC_MAXD][64];
     double w[ORC_MAXD][64];
     const int W = p->W, d = p->d;
     node_setup(p, xj, u, w);
+    for (int t = 0; t < d; ++t)
+        for (int l = 0; l < W; ++l) ix[t][l] = wrap(u[t] + l, p->n[t]);
     if (d == 1) {
         for (int l0 = 0; l0 < W; ++l0) {
-            int64_t i0 = wrap(u[0] + l0, p->n[0]);
-            g[2 * i0] += fj[0] * w[0][l0];
-            g[2 * i0 + 1] += fj[1] * w[0][l0];
+            double *gp = g + 2 * ix[0][l0];
+            gp[0] += fj[0] * w[0][l0];
+            gp[1] += fj[1] * w[0][l0];
         }
     } else if (d == 2) {
         for (int l0 = 0; l0 < W; ++l0) {
-            int64_t i0 = wrap(u[0] + l0, p->n[0]);
+            double *row = g + 2 * ix[0][l0] * p->n[1];
             for (int l1 = 0; l1 < W; ++l1) {
-                int64_t gi = i0 * p->n[1] + wrap(u[1] + l1, p->n[1]);
-                g[2 * gi] += fj[0] * w[1][l1] * w[0][l0];
-                g[2 * gi + 1] += fj[1] * w[1][l1] * w[0][l0];
+                double *gp = row + 2 * ix[1][l1];
+                gp[0] += fj[0] * w[1][l1] * w[0][l0];
+                gp[1] += fj[1] * w[1][l1] * w[0][l0];
             }
         }
     } else {
         for (int l0 = 0; l0 < W; ++l0) {
-            int64_t i0 = wrap(u[0] + l0, p->n[0]);
             for (int l1 = 0; l1 < W; ++l1) {
-                int64_t i1 = wrap(u[1] + l1, p->n[1]);
+                double *row = g + 2 * (ix[0][l0] * p->n[1] + ix[1][l1]) * p->n[2];
+                const double a0 = fj[0] * w[0][l0] * w[1][l1], a1 = fj[1] * w[0][l0] * w[1][l1];
                 for (int l2 = 0; l2 < W; ++l2) {
-                    int64_t gi = (i0 * p->n[1] + i1) * p->n[2] + wrap(u[2] + l2, p->n[2]);
-                    g[2 * gi] += fj[0] * w[0][l0] * w[1][l1] * w[2][l2];
-                    g[2 * gi + 1] += fj[1] * w[0][l0] * w[1][l1] * w[2][l2];
+                    double *gp = row + 2 * ix[2][l2];
+                    gp[0] += a0 * w[2][l2];
+                    gp[1] += a1 * w[2][l2];
                 }
             }
         }

@@ -1,0 +1,396 @@
+"""GPU parity: the CUDA path through the C-ABI against the CPU oracle and the reference's KATs.
+
+Tolerances: FP64 form within 1e-12 relative l2 of the oracle's restatement of
+the reference method (same window, m, n and index rule); FP32 form within 1e-5
+relative l2 of the FP64 result; direct NDFT within 1e-11.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden", "kats.json")
+KATS = json.load(open(GOLD))["kats"]
+
+TOL64 = 1e-12
+TOL32 = 1e-5
+TOL_NDFT = 1e-11
+
+
+@pytest.fixture(scope="module")
+def dev():
+    from cunfft_gb300 import _native
+    _native.lib()
+    return torch.device("cuda:0")
+
+
+def _rand(shape, rng):
+    return rng.uniform(-1, 1, shape) + 1j * rng.uniform(-1, 1, shape)
+
+
+def _kat_subset():
+    out = []
+    for k in KATS:
+        cost = k["M"] * int(np.prod(k["N"]))
+        if cost <= 2e7 and (k["N"][0] in (16, 64, 256, 4096) or k["d"] == 3):
+            out.append(k)
+    return out
+
+
+def _kid(k):
+    return f"{k['direction'][:3]}-m{k['m']}-d{k['d']}-N{k['N'][0]}"
+
+
+# ---------------------------------------------------------------------------
+# Reference-style driver through the drop-in ABI: known answers
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("k", _kat_subset(), ids=_kid)
+def test_abi_reproduces_reference_kat(dev, k):
+    from cunfft_gb300.abi import ReferencePlan
+
+    N, M, m = k["N"], k["M"], k["m"]
+    adj = k["direction"] == "adjoint"
+    x, c = O.reference_example_data(N, M, adj, k["skip_generations"])
+    p = ReferencePlan(N, M, m=m)
+    assert p.plan.m == m and list(p.plan.n[i] for i in range(len(N))) == O.default_n(N)
+    p.x[:] = x
+    if not adj:
+        p.f_hat[:] = c
+        p.copyDataToDevice()
+        p.cundft_transform()
+        nd = p.copy_f_ToHost()
+        p.cunfft_reinit()
+        p.copyDataToDevice()
+        p.cunfft_transform()
+        p.copyDataToHost()
+        got = p.f.copy()
+        ref_nfft = O.nfft_forward(x, c, N, m=m)
+        ref_ndft = O.ndft_forward(x, c, N)
+    else:
+        p.f[:] = c
+        p.copyDataToDeviceAd()
+        p.cundft_adjoint()
+        nd = p.copy_f_hat_ToHost()
+        p.cunfft_reinitAd()
+        p.copyDataToDeviceAd()
+        p.cunfft_adjoint()
+        p.copyDataToHostAd()
+        got = p.f_hat.copy()
+        ref_nfft = O.nfft_adjoint(x, c, N, m=m).reshape(-1)
+        ref_ndft = O.ndft_adjoint(x, c, N).reshape(-1)
+    p.check()
+    times = p.times
+    p.cunfft_finalize()
+    assert O.rel_l2(ref_nfft, got) < TOL64
+    assert O.rel_l2(ref_ndft, nd) < TOL_NDFT
+    e = O.error_l_infty(nd, got)
+    tol = 1e-3 if m <= 8 else 1e-2
+    assert abs(e / k["e_inf"] - 1) < tol, (e, k["e_inf"])
+    assert times["time_FFT"] > 0 and times["time_CONV"] > 0
+
+
+def test_abi_reference_driver_flow_with_library_example_data(dev):
+    """getExampleData_uniDistr of the library draws the same drand48 stream as the reference."""
+    from cunfft_gb300.abi import ReferencePlan
+
+    p = ReferencePlan([32, 32], 1024)
+    p.getExampleData_uniDistr()
+    x, fh = p.x.copy(), p.f_hat.copy()
+    p.copyDataToDevice()
+    p.cunfft_transform()
+    p.copyDataToHost()
+    assert O.rel_l2(O.nfft_forward(x, fh, [32, 32]), p.f) < TOL64
+    assert np.array_equal(p.copy_x_toHost(), x)
+    p.cunfft_finalize()
+
+
+def test_abi_initguru_custom_n_and_flags(dev):
+    from cunfft_gb300 import _native as nat
+    from cunfft_gb300.abi import ReferencePlan
+
+    rng = np.random.default_rng(11)
+    N, n, M = [24, 40], [64, 128], 700
+    x = rng.uniform(-0.5, 0.5, (M, 2))
+    fh = _rand(N, rng).reshape(-1)
+    for flags in (nat.CUFFT_INIT | nat.CUFFT_BOTH, nat.CUFFT_INIT | nat.CUFFT_FORW | nat.CUFFT_BACKW, 0):
+        p = ReferencePlan(N, M, n=n, flags=flags)
+        p.x[:] = x
+        p.f_hat[:] = fh
+        p.copyDataToDevice()
+        p.cunfft_transform()
+        p.copyDataToHost()
+        p.check()
+        assert O.rel_l2(O.nfft_forward(x, fh, N, n=n), p.f) < TOL64
+        p.cunfft_finalize()
+
+
+def test_abi_two_plans_coexist(dev):
+    """No global plan state: two plans of different shapes interleave."""
+    from cunfft_gb300.abi import ReferencePlan
+
+    rng = np.random.default_rng(2)
+    a = ReferencePlan([64], 300)
+    b = ReferencePlan([16, 8, 8], 500)
+    xa, xb = rng.uniform(-0.5, 0.5, (300, 1)), rng.uniform(-0.5, 0.5, (500, 3))
+    fa, fb = _rand(64, rng), _rand(16 * 8 * 8, rng)
+    a.x[:] = xa; a.f_hat[:] = fa
+    b.x[:] = xb; b.f_hat[:] = fb
+    a.copyDataToDevice(); b.copyDataToDevice()
+    a.cunfft_transform(); b.cunfft_transform()
+    a.copyDataToHost(); b.copyDataToHost()
+    assert O.rel_l2(O.nfft_forward(xa, fa, [64]), a.f) < TOL64
+    assert O.rel_l2(O.nfft_forward(xb, fb, [16, 8, 8]), b.f) < TOL64
+    a.cunfft_finalize()
+    b.cunfft_finalize()
+
+
+# ---------------------------------------------------------------------------
+# Extension API: FP64 and FP32 forms against the oracle
+# ---------------------------------------------------------------------------
+CASES = [
+    ([64], 1000, 6), ([4096], 5000, 6), ([33], 257, 4), ([128], 4000, 12),
+    ([64, 64], 4096, 6), ([48, 80], 3000, 5), ([32, 32], 2048, 2), ([16, 16], 600, 12), ([40, 24], 1500, 8),
+    ([16, 16, 16], 4096, 6), ([8, 16, 12], 2000, 5), ([16, 8, 32], 3000, 3), ([8, 8, 8], 500, 12),
+]
+
+
+def _cid(c):
+    return f"N{'x'.join(map(str, c[0]))}-M{c[1]}-m{c[2]}"
+
+
+@pytest.mark.parametrize("case", CASES, ids=_cid)
+def test_x_forward_adjoint_match_oracle(dev, case):
+    from cunfft_gb300.nfft import NFFT
+
+    N, M, m = case
+    rng = np.random.default_rng(sum(N) + M + m)
+    x = rng.uniform(-0.5, 0.5, (M, len(N)))
+    fh = _rand(N, rng)
+    f = _rand(M, rng)
+    ref_f = O.nfft_forward(x, fh, N, m=m)
+    ref_fh = O.nfft_adjoint(x, f, N, m=m)
+    xt = torch.from_numpy(x).to(dev)
+    for prec, tol in (("f64", TOL64), ("f32", TOL32)):
+        p = NFFT(N, m=m, precision=prec, device=dev).set_nodes(xt)
+        got_f = p.forward(torch.from_numpy(fh).to(dev)).cpu().numpy()
+        got_fh = p.adjoint(torch.from_numpy(f).to(dev)).cpu().numpy()
+        assert O.rel_l2(ref_f, got_f) < tol, prec
+        assert O.rel_l2(ref_fh, got_fh) < tol, prec
+        p.close()
+
+
+def test_x_ndft_matches_oracle(dev):
+    from cunfft_gb300.nfft import NFFT
+
+    rng = np.random.default_rng(5)
+    for N, M in (([100], 333), ([24, 16], 500), ([8, 6, 10], 400)):
+        x = rng.uniform(-0.5, 0.5, (M, len(N)))
+        fh, f = _rand(N, rng), _rand(M, rng)
+        p = NFFT(N, device=dev).set_nodes(torch.from_numpy(x).to(dev))
+        assert O.rel_l2(O.ndft_forward(x, fh, N), p.ndft_forward(torch.from_numpy(fh).to(dev)).cpu()) < TOL_NDFT
+        assert O.rel_l2(O.ndft_adjoint(x, f, N), p.ndft_adjoint(torch.from_numpy(f).to(dev)).cpu()) < TOL_NDFT
+        p.close()
+
+
+# ---------------------------------------------------------------------------
+# Edge cases the reference exercises or leaves undefined
+# ---------------------------------------------------------------------------
+def test_edge_nodes_boundaries_ties_and_signed_zero(dev):
+    from cunfft_gb300.nfft import NFFT
+
+    n = 128
+    special = [-0.5, -0.0, 0.0, 0.5 - 2 ** -40, 2.5 / n, -2.5 / n, 3.5 / n, 0.25, -0.25, 1e-300, -1e-300]
+    rng = np.random.default_rng(9)
+    x = np.array([[a, b] for a in special for b in special])
+    fh = _rand([64, 64], rng)
+    f = _rand(len(x), rng)
+    p = NFFT([64, 64], device=dev).set_nodes(torch.from_numpy(x).to(dev))
+    assert O.rel_l2(O.nfft_forward(x, fh, [64, 64]), p.forward(torch.from_numpy(fh).to(dev)).cpu()) < TOL64
+    assert O.rel_l2(O.nfft_adjoint(x, f, [64, 64]), p.adjoint(torch.from_numpy(f).to(dev)).cpu()) < TOL64
+    p.close()
+
+
+def test_edge_empty_and_single_node(dev):
+    from cunfft_gb300.nfft import NFFT
+
+    rng = np.random.default_rng(4)
+    fh = _rand([16, 16], rng)
+    p = NFFT([16, 16], device=dev)
+    p.set_nodes(torch.zeros((0, 2), dtype=torch.float64, device=dev))
+    assert p.forward(torch.from_numpy(fh).to(dev)).numel() == 0
+    out = p.adjoint(torch.zeros(0, dtype=torch.complex128, device=dev))
+    assert torch.count_nonzero(out).item() == 0
+    x = np.array([[0.1, -0.3]])
+    p.set_nodes(torch.from_numpy(x).to(dev))
+    assert O.rel_l2(O.nfft_forward(x, fh, [16, 16]), p.forward(torch.from_numpy(fh).to(dev)).cpu()) < TOL64
+    p.close()
+
+
+def test_edge_window_wider_than_grid(dev):
+    """m = 12 on an n = 16 grid: 26 taps wrap around the grid more than once."""
+    from cunfft_gb300.nfft import NFFT
+
+    rng = np.random.default_rng(8)
+    for N in ([8], [8, 8], [8, 8, 8]):
+        M = 100
+        x = rng.uniform(-0.5, 0.5, (M, len(N)))
+        fh, f = _rand(N, rng), _rand(M, rng)
+        for prec, tol in (("f64", TOL64), ("f32", TOL32)):
+            p = NFFT(N, m=12, precision=prec, device=dev).set_nodes(torch.from_numpy(x).to(dev))
+            assert O.rel_l2(O.nfft_forward(x, fh, N, m=12), p.forward(torch.from_numpy(fh).to(dev)).cpu()) < tol
+            assert O.rel_l2(O.nfft_adjoint(x, f, N, m=12), p.adjoint(torch.from_numpy(f).to(dev)).cpu()) < tol
+            p.close()
+
+
+def test_edge_clustered_nodes_split_into_work_items(dev):
+    """Thousands of nodes in one tile: the tile is split into many work items."""
+    from cunfft_gb300.nfft import NFFT
+
+    rng = np.random.default_rng(12)
+    M = 20000
+    x = np.clip(rng.normal(0, 0.002, (M, 2)), -0.5, 0.4999)
+    x[:50] = 0.123  # identical nodes
+    fh, f = _rand([64, 64], rng), _rand(M, rng)
+    for prec, tol in (("f64", TOL64), ("f32", TOL32)):
+        p = NFFT([64, 64], precision=prec, device=dev).set_nodes(torch.from_numpy(x).to(dev))
+        p.set_tiling([32, 32], chunk=256)
+        assert O.rel_l2(O.nfft_forward(x, fh, [64, 64]), p.forward(torch.from_numpy(fh).to(dev)).cpu()) < tol
+        assert O.rel_l2(O.nfft_adjoint(x, f, [64, 64]), p.adjoint(torch.from_numpy(f).to(dev)).cpu()) < tol
+        p.close()
+
+
+@pytest.mark.parametrize("d", [1, 2, 3])
+def test_tilings_agree(dev, d):
+    from cunfft_gb300.nfft import NFFT
+
+    rng = np.random.default_rng(d)
+    N = [[256], [32, 64], [16, 16, 32]][d - 1]
+    M = 3000
+    x = rng.uniform(-0.5, 0.5, (M, d))
+    fh, f = _rand(N, rng), _rand(M, rng)
+    ref_f, ref_fh = O.nfft_forward(x, fh, N), O.nfft_adjoint(x, f, N)
+    tilings = {1: [[16], [64], [512]], 2: [[4, 8], [16, 16], [64, 32]], 3: [[4, 4, 4], [8, 4, 16], [16, 16, 16]]}[d]
+    for T in tilings:
+        for chunk in (64, 4096):
+            p = NFFT(N, device=dev).set_nodes(torch.from_numpy(x).to(dev))
+            p.set_tiling(T, chunk)
+            assert p.tiling()["T"] == T
+            assert O.rel_l2(ref_f, p.forward(torch.from_numpy(fh).to(dev)).cpu()) < TOL64
+            assert O.rel_l2(ref_fh, p.adjoint(torch.from_numpy(f).to(dev)).cpu()) < TOL64
+            p.close()
+
+
+# ---------------------------------------------------------------------------
+# Batched instances with uneven node counts
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("prec,tol", [("f64", TOL64), ("f32", TOL32)])
+def test_batched_uneven(dev, prec, tol):
+    from cunfft_gb300.nfft import NFFT
+
+    rng = np.random.default_rng(21)
+    N = [32, 32]
+    Ms = [0, 17, 1000, 1, 2500, 0, 640]
+    B = len(Ms)
+    xs = [rng.uniform(-0.5, 0.5, (M, 2)) for M in Ms]
+    fhs = [_rand(N, rng) for _ in Ms]
+    fs = [_rand(M, rng) for M in Ms]
+    p = NFFT(N, m=5, precision=prec, batch=B, device=dev)
+    p.set_nodes(torch.from_numpy(np.concatenate(xs)).to(dev), Ms)
+    got_f = p.forward(torch.from_numpy(np.stack(fhs)).to(dev)).cpu().numpy()
+    got_fh = p.adjoint(torch.from_numpy(np.concatenate(fs)).to(dev)).cpu().numpy()
+    off = 0
+    for i, M in enumerate(Ms):
+        if M:
+            assert O.rel_l2(O.nfft_forward(xs[i], fhs[i], N, m=5), got_f[off:off + M]) < tol
+            assert O.rel_l2(O.nfft_adjoint(xs[i], fs[i], N, m=5), got_fh[i]) < tol
+        else:
+            assert np.count_nonzero(got_fh[i]) == 0
+        off += M
+    # batched NDFT as well
+    nd = p.ndft_forward(torch.from_numpy(np.stack(fhs)).to(dev)).cpu().numpy()
+    off = 0
+    for i, M in enumerate(Ms):
+        if M:
+            assert O.rel_l2(O.ndft_forward(xs[i], fhs[i], N), nd[off:off + M]) < TOL_NDFT
+        off += M
+    p.close()
+
+
+# ---------------------------------------------------------------------------
+# Properties at the benchmark's full size (3D N = 128^3, M = 2^21)
+# ---------------------------------------------------------------------------
+def test_full_size_3d_properties(dev):
+    from cunfft_gb300.nfft import NFFT
+
+    g = torch.Generator(device=dev).manual_seed(1)
+    N, M = [128, 128, 128], 1 << 21
+    x = torch.rand(M, 3, generator=g, device=dev, dtype=torch.float64) - 0.5
+    fh = torch.complex(torch.rand(N, generator=g, device=dev, dtype=torch.float64) * 2 - 1,
+                       torch.rand(N, generator=g, device=dev, dtype=torch.float64) * 2 - 1)
+    f = torch.complex(torch.rand(M, generator=g, device=dev, dtype=torch.float64) * 2 - 1,
+                      torch.rand(M, generator=g, device=dev, dtype=torch.float64) * 2 - 1)
+    p32 = NFFT(N, precision="f32", device=dev).set_nodes(x)
+    Af = p32.forward(fh).to(torch.complex128)
+    AHf = p32.adjoint(f).to(torch.complex128)
+    # adjointness <A fh, f> = <fh, A^H f>
+    lhs = torch.vdot(Af, f)
+    rhs = torch.vdot(fh.reshape(-1), AHf.reshape(-1))
+    assert abs(lhs - rhs) / abs(lhs) < 1e-5
+    # accuracy against the FP64 NDFT on a 4096-node subsample (forward) and
+    # a 4096-coefficient check on a node subsample via adjointness is above
+    idx = torch.randperm(M, generator=g, device=dev)[:4096]
+    sub = NFFT(N, device=dev).set_nodes(x[idx].contiguous())
+    nd = sub.ndft_forward(fh)
+    assert (torch.linalg.norm(nd - Af[idx]) / torch.linalg.norm(nd)).item() < 1e-5
+    # FP64 form on the same subsample of nodes (all taps exercised)
+    f64 = sub.forward(fh)
+    assert (torch.linalg.norm(nd - f64) / torch.linalg.norm(nd)).item() < 1e-6
+    # linearity of the adjoint
+    a, b = 0.75 - 0.5j, -1.25 + 0.25j
+    f2 = torch.roll(f, 12345)
+    lin = p32.adjoint(a * f + b * f2).to(torch.complex128)
+    ref = a * AHf + b * p32.adjoint(f2).to(torch.complex128)
+    assert (torch.linalg.norm(lin - ref) / torch.linalg.norm(ref)).item() < 1e-5
+    p32.close()
+    sub.close()
+
+
+# ---------------------------------------------------------------------------
+# Autotuner and stage timing
+# ---------------------------------------------------------------------------
+def test_autotune_keeps_results(dev):
+    from cunfft_gb300.nfft import NFFT
+
+    rng = np.random.default_rng(31)
+    N, M = [32, 32, 32], 20000
+    x = rng.uniform(-0.5, 0.5, (M, 3))
+    fh, f = _rand(N, rng), _rand(M, rng)
+    p = NFFT(N, precision="f32", device=dev).set_nodes(torch.from_numpy(x).to(dev))
+    t = p.autotune(reps=1)
+    assert len(t["T"]) == 3
+    assert O.rel_l2(O.nfft_forward(x, fh, N), p.forward(torch.from_numpy(fh).to(dev)).cpu()) < TOL32
+    assert O.rel_l2(O.nfft_adjoint(x, f, N), p.adjoint(torch.from_numpy(f).to(dev)).cpu()) < TOL32
+    st = p.stage_times()
+    assert st["fft"] > 0 and st["conv"] > 0
+    p.close()
+
+
+def test_errors_are_status_codes(dev):
+    from cunfft_gb300 import _native as nat
+    from cunfft_gb300.nfft import NFFT
+
+    with pytest.raises(nat.CunfftError):
+        NFFT([10], n=[24], device=dev)  # n not a power of two
+    with pytest.raises(nat.CunfftError):
+        NFFT([10], m=16, device=dev)
+    p = NFFT([16], device=dev)
+    with pytest.raises(nat.CunfftError) as ei:
+        p.forward(torch.zeros(16, dtype=torch.complex128, device=dev))
+    assert ei.value.status == nat.NODES_NOT_SET
+    p.close()
