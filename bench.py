@@ -46,7 +46,56 @@ def parse_args():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--case", choices=["interp", "spread", "step"],
+                    help="profiling case: bind nodes once, then launch only this stage (3 times)")
+    ap.add_argument("--precision", default="f32", choices=["f32", "f64"])
+    ap.add_argument("--M", type=int, default=M_FULL)
+    ap.add_argument("--tile", default="", help="tile extents for --case, e.g. 8,4,16")
     return ap.parse_args()
+
+
+def run_case(args):
+    """A few launches of one stage on the benchmark workload, for ncu captures."""
+    import torch
+
+    from cunfft_gb300.nfft import NFFT
+
+    dev = torch.device("cuda", 0)
+    g = torch.Generator(device=dev).manual_seed(20240)
+    M = args.M
+    x = torch.rand(M, 3, generator=g, device=dev, dtype=torch.float64) - 0.5
+    cd = torch.complex64 if args.precision == "f32" else torch.complex128
+    fh = torch.complex(torch.rand(N3, generator=g, device=dev, dtype=torch.float64) * 2 - 1,
+                       torch.rand(N3, generator=g, device=dev, dtype=torch.float64) * 2 - 1).to(cd)
+    f = torch.complex(torch.rand(M, generator=g, device=dev, dtype=torch.float64) * 2 - 1,
+                      torch.rand(M, generator=g, device=dev, dtype=torch.float64) * 2 - 1).to(cd)
+    p = NFFT(N3, m=M_CUT, precision=args.precision, device=dev)
+    if args.tile:
+        p.set_tiling([int(v) for v in args.tile.split(",")])
+    p.set_nodes(x)
+    grid = p.grid()
+    out = torch.empty(M, dtype=cd, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    times = []
+    for _ in range(3):
+        if args.case == "spread":
+            grid.zero_()
+        a.record(stream)
+        if args.case == "interp":
+            p.interp(grid, out=out)
+        elif args.case == "spread":
+            p.spread(f, grid)
+        else:
+            p.set_nodes(x)
+            p.forward(fh, out=out)
+            p.adjoint(f)
+        b.record(stream)
+        b.synchronize()
+        times.append(a.elapsed_time(b))
+    print(json.dumps({"case": args.case, "precision": args.precision, "M": M, "tiling": p.tiling(),
+                      "ms": times}))
+    p.close()
 
 
 def dist_env():
@@ -447,7 +496,9 @@ def run_reference(args):
 
 def main():
     args = parse_args()
-    if args.impl == "reference":
+    if args.case:
+        run_case(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -48,6 +48,7 @@ struct Tiling {
   int chunk;             // max nodes per work item
   int threads;           // CTA size of the gridding kernels
   size_t smem_tile;      // bytes of the staged tile
+  int use_global;        // 1: no shared-memory tile fits, grid in global memory
 };
 
 // Sorted node records, produced by the binning kernels.

@@ -1,5 +1,5 @@
 // grid_dispatch.cu -- selects the gridding kernel instance for the plan's tap count.
-#include "runtime.h"
+#include "kernels_grid.cuh"
 
 namespace cg {
 
@@ -10,15 +10,20 @@ CG_DECL(20) CG_DECL(22) CG_DECL(24) CG_DECL(26) CG_DECL(28) CG_DECL(30) CG_DECL(
 
 bool gridding_supported(int d, int W) { return d >= 1 && d <= 3 && W >= 4 && W <= 32 && (W % 2) == 0; }
 
+// Larger of the interpolation and spreading kernels' shared-memory needs.
 size_t gridding_smem_bytes(const Plan& p) {
   const int d = p.geo.d, W = p.geo.W;
-  const size_t elem = p.prec == kF64 ? 16 : 8, real = elem / 2;
+  const size_t real = p.prec == kF64 ? 8 : 4;
   const int nwarps = p.tl.threads / 32;
-  const int nb = d == 1 ? 32 : 32 / d;
-  return p.tl.smem_tile + (size_t)nwarps * nb * d * W * real;
+  const size_t a = grid_extra_smem(d, W, real, nwarps, p.tl.smem_tile, false);
+  const size_t b = grid_extra_smem(d, W, real, nwarps, p.tl.smem_tile, true);
+  return p.tl.smem_tile + (a > b ? a : b);
 }
 
+cudaError_t grid_launch_global(const Plan&, bool, const void*, void*, cudaStream_t);
+
 static cudaError_t dispatch(const Plan& p, bool spread, const void* in, void* out, cudaStream_t st) {
+  if (p.tl.use_global) return grid_launch_global(p, spread, in, out, st);
   switch (p.geo.W) {
 #define CG_CASE(W) case W: return grid_launch_w##W(p, spread, in, out, st);
     CG_CASE(4) CG_CASE(6) CG_CASE(8) CG_CASE(10) CG_CASE(12) CG_CASE(14) CG_CASE(16) CG_CASE(18)

@@ -11,6 +11,9 @@
 
 namespace cg {
 
+// bits per dimension of the packed tile-local window start (30 / d)
+__host__ __device__ inline int off_bits_host(int d) { return d == 1 ? 30 : (d == 2 ? 15 : 10); }
+
 __device__ __forceinline__ int find_instance(const int32_t* __restrict__ inst_off, int batch, int64_t j) {
   int lo = 0, hi = batch;  // inst_off[lo] <= j < inst_off[hi]
   while (hi - lo > 1) {
@@ -59,7 +62,7 @@ __global__ void k_bin_scatter(const double* __restrict__ x, int64_t M, Geom geo,
       reduce_coord(x[j * d + t], geo.n[t], geo.m, u, c);
       int64_t s = wrap_pow2(u, geo.n[t]);
       uint32_t o = (uint32_t)(s % tl.T[t]);
-      packed |= o << (10 * t);
+      packed |= o << (off_bits_host(d) * t);
       sfrac[pos * d + t] = (T)(c - (double)geo.m);
     }
     sidx[pos] = (int32_t)j;

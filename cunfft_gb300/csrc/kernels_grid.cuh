@@ -12,23 +12,30 @@
 //  * The CTA stages the padded tile (T_t + W - 1 per dim, wrapped mod n) in shared
 //    memory.  Row stride S == W (mod 16) elements, so the lane -> tap mapping below
 //    touches consecutive shared-memory banks: no bank conflicts for 8-byte
-//    (float2) or 16-byte (double2) elements.
-//  * One warp per node at a time.  Lane i < R*W (R = 32/W) owns innermost tap
-//    l_last = i % W and rows r = i / W, r + R, r + 2R, ... of the remaining taps;
-//    for d = 3 each row is a (l0, l1) pair and the lane loops over the 2m+2 planes
-//    l0 with the plane weights held in registers.  The warp reduces the node's
-//    sum with shuffles (interpolation) or adds the taps into the staged tile with
-//    shared-memory atomics (spreading); the spread tile is then added to the
-//    global grid with vector atomics, so neighbouring items' halos combine.
-//  * Tap weights of a batch of 32/d nodes are computed by lane (node, dim) pairs
-//    and parked in shared memory: exp2f per tap in the FP32 form; in the FP64 form
-//    the reference's fast-Gaussian-gridding recurrence (2 exp per node and dim,
-//    src/cunfft_kernel.cu:491-505), which keeps the scarce FP64 pipe on the taps.
+//    (float2) or 16-byte (double2) elements.  All shared-memory indices are 32-bit.
+//  * Lane i < R*W (R = 32/W) owns innermost tap l_last = i % W and rows
+//    r = i / W, r + R, ... of the remaining taps (for d = 3 a row is an (l0, l1)
+//    pair walked over the 2m+2 planes l0).
+//  * Interpolation: one warp per node at a time; the warp reduces the node's sum
+//    with shuffles.  Node records and tap weights of a batch of nodes are staged
+//    per warp in shared memory, so the tap loop does no global loads.
+//  * Spreading: no shared-memory atomics (a float atomic add on shared memory is a
+//    compare-and-swap loop).  Every warp walks all nodes of a CTA-wide batch but
+//    writes only the planes (d = 3) or row groups (d = 2) it owns, with plain
+//    load / FMA / store; for d = 1 each warp accumulates into a private copy of
+//    the tile.  The tile is then added to the global grid with vector atomics, so
+//    neighbouring items' halos combine.
+//  * Tap weights: exp2f per tap in the FP32 form; in the FP64 form the reference's
+//    fast-Gaussian-gridding recurrence (2 exp per node and dim, src/cunfft_kernel.cu:
+//    491-505), which keeps the scarce FP64 pipe on the taps.
 #pragma once
 
 #include "runtime.h"
 
 namespace cg {
+
+// bits of the packed tile-local window start, per dimension
+__host__ __device__ constexpr int off_bits(int d) { return d == 1 ? 30 : (d == 2 ? 15 : 10); }
 
 template <typename T> struct WeightMath;
 
@@ -38,7 +45,7 @@ template <> struct WeightMath<float> {
     const float cb = (float)(1.4426950408889634 / b);
 #pragma unroll 4
     for (int l = 0; l < W; ++l) {
-      float y = fr + (float)(m - l);
+      const float y = fr + (float)(m - l);
       out[l] = exp2f(-(y * y) * cb);
     }
   }
@@ -51,7 +58,7 @@ template <> struct WeightMath<double> {
     const double ib = 1.0 / b;
     const double phi = exp(-(c * c) * ib);
     const double E = exp(2.0 * c * ib);
-    const double q = exp(-ib);           // exp(-l^2/b) by the recurrence of src/cunfft.cu:60-76
+    const double q = exp(-ib);            // exp(-l^2/b) by the recurrence of src/cunfft.cu:60-76
     double e = 1.0, gl = 1.0, qstep = q;  // gl = exp(-l^2/b), qstep = exp(-(2l+1)/b)
     out[0] = phi;
 #pragma unroll 4
@@ -82,95 +89,113 @@ __device__ __forceinline__ void global_add(double2* p, double2 v) {
 }
 
 template <typename C>
-__device__ __forceinline__ C shfl_xor_c(C v, int o);
-template <>
-__device__ __forceinline__ float2 shfl_xor_c<float2>(float2 v, int o) {
-  return make_float2(__shfl_xor_sync(0xffffffffu, v.x, o), __shfl_xor_sync(0xffffffffu, v.y, o));
-}
-template <>
-__device__ __forceinline__ double2 shfl_xor_c<double2>(double2 v, int o) {
-  return make_double2(__shfl_xor_sync(0xffffffffu, v.x, o), __shfl_xor_sync(0xffffffffu, v.y, o));
+__device__ __forceinline__ C czero() {
+  C z;
+  z.x = 0;
+  z.y = 0;
+  return z;
 }
 
-// Decode the work item's tile into instance and tile origin a_t.
+template <typename C>
+__device__ __forceinline__ C shfl_xor_c(C v, int o) {
+  v.x = __shfl_xor_sync(0xffffffffu, v.x, o);
+  v.y = __shfl_xor_sync(0xffffffffu, v.y, o);
+  return v;
+}
+
+__device__ __forceinline__ double geo_b(const Geom& g, int t) { return t == 0 ? g.b[0] : (t == 1 ? g.b[1] : g.b[2]); }
+
+// Tile origin a_t of a work item's tile and its instance.
 struct TileOrigin {
   int64_t inst;
   int64_t a[kMaxDim];
 };
 
+template <int D>
 __device__ __forceinline__ TileOrigin decode_tile(const Geom& geo, const Tiling& tl, int64_t tile) {
   TileOrigin o;
   o.inst = tile / tl.tiles_per_inst;
   int64_t lt = tile - o.inst * tl.tiles_per_inst;
-  for (int t = geo.d - 1; t >= 0; --t) {
-    int64_t b = lt % tl.nb[t];
-    lt /= tl.nb[t];
-    o.a[t] = b * tl.T[t];
+  o.a[0] = o.a[1] = o.a[2] = 0;
+  if (D == 3) {
+    o.a[2] = (lt % tl.nb[2]) * tl.T[2];
+    lt /= tl.nb[2];
   }
+  if (D >= 2) {
+    o.a[1] = (lt % tl.nb[1]) * tl.T[1];
+    lt /= tl.nb[1];
+  }
+  o.a[0] = lt * tl.T[0];
   return o;
 }
 
-// Shared-memory layout: [E0][E1][S] (d = 3), [E0][S] (d = 2), [S] (d = 1) complex
-// elements, followed by the per-warp weight buffers [nwarps][32/d][d][W] of T.
+// Rows of the staged tile: [E0][E1] for d = 3, [E0] for d = 2, one for d = 1.
+template <int D>
+__device__ __forceinline__ int tile_rows(const Tiling& tl) {
+  return D == 3 ? tl.E[0] * tl.E[1] : (D == 2 ? tl.E[0] : 1);
+}
+
+template <int D>
+__device__ __forceinline__ int64_t row_base(const Geom& geo, const Tiling& tl, const TileOrigin& o, int row) {
+  if (D == 3) {
+    const int p0 = row / tl.E[1], p1 = row - p0 * tl.E[1];
+    return (wrap_pow2(o.a[0] + p0, geo.n[0]) * geo.n[1] + wrap_pow2(o.a[1] + p1, geo.n[1])) * geo.n[2];
+  }
+  if (D == 2) return wrap_pow2(o.a[0] + row, geo.n[0]) * geo.n[1];
+  return 0;
+}
+
 template <int D, typename C>
 __device__ __forceinline__ void load_tile(C* tile, const C* __restrict__ gi, const Geom& geo, const Tiling& tl,
-                                          const TileOrigin& o, int warp, int nwarps, int lane) {
+                                          const TileOrigin& o) {
   const int E_last = tl.E[D - 1];
-  const int64_t n_last = geo.n[D - 1];
+  const int64_t n_last = geo.n[D - 1], a_last = o.a[D - 1];
   if (D == 1) {
-    for (int p = threadIdx.x; p < E_last; p += blockDim.x) tile[p] = gi[wrap_pow2(o.a[0] + p, n_last)];
+    for (int p = threadIdx.x; p < E_last; p += blockDim.x) tile[p] = gi[wrap_pow2(a_last + p, n_last)];
     return;
   }
-  const int rows = D == 3 ? tl.E[0] * tl.E[1] : tl.E[0];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int rows = tile_rows<D>(tl);
   for (int row = warp; row < rows; row += nwarps) {
-    int64_t gbase;
-    if (D == 3) {
-      const int p0 = row / tl.E[1], p1 = row - p0 * tl.E[1];
-      gbase = (wrap_pow2(o.a[0] + p0, geo.n[0]) * geo.n[1] + wrap_pow2(o.a[1] + p1, geo.n[1])) * geo.n[2];
-    } else {
-      gbase = wrap_pow2(o.a[0] + row, geo.n[0]) * geo.n[1];
-    }
-    C* dst = tile + (int64_t)row * tl.S;
-    for (int p = lane; p < E_last; p += kWarp) dst[p] = gi[gbase + wrap_pow2(o.a[D - 1] + p, n_last)];
+    const int64_t gbase = row_base<D>(geo, tl, o, row);
+    C* dst = tile + row * tl.S;
+    for (int p = lane; p < E_last; p += kWarp) dst[p] = gi[gbase + wrap_pow2(a_last + p, n_last)];
   }
 }
 
+// Add the tile into the global grid.  FP32 pairs (even offset, so 16-byte
+// aligned and never split by the power-of-two wrap) go as one float4 atomic.
 template <int D, typename C>
 __device__ __forceinline__ void flush_tile(const C* tile, C* __restrict__ gi, const Geom& geo, const Tiling& tl,
-                                           const TileOrigin& o, int warp, int nwarps, int lane) {
+                                           const TileOrigin& o) {
   const int E_last = tl.E[D - 1];
-  const int64_t n_last = geo.n[D - 1];
-  if (D == 1) {
-    for (int p = threadIdx.x; p < E_last; p += blockDim.x) {
-      C v = tile[p];
-      if (v.x != 0 || v.y != 0) global_add(&gi[wrap_pow2(o.a[0] + p, n_last)], v);
+  const int64_t n_last = geo.n[D - 1], a_last = o.a[D - 1];
+  const int rows = tile_rows<D>(tl);
+  constexpr bool kF32 = sizeof(C) == 8;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  if (kF32 && n_last >= 2 && (tl.T[D - 1] & 1) == 0) {  // even tile origin: pairs stay 16-byte aligned
+    const int pairs = (E_last + 1) >> 1;
+    const int total = rows * pairs;
+    for (int e = tid; e < total; e += nt) {
+      const int row = e / pairs, pp = e - row * pairs, p = 2 * pp;
+      const C* src = tile + row * tl.S + p;
+      const int64_t gidx = row_base<D>(geo, tl, o, row) + wrap_pow2(a_last + p, n_last);
+      const C v0 = src[0];
+      if (p + 1 < E_last) {
+        const C v1 = src[1];
+        if (v0.x != 0 || v0.y != 0 || v1.x != 0 || v1.y != 0)
+          atomicAdd(reinterpret_cast<float4*>(gi + gidx), make_float4(v0.x, v0.y, v1.x, v1.y));
+      } else if (v0.x != 0 || v0.y != 0) {
+        global_add(gi + gidx, v0);
+      }
     }
     return;
   }
-  const int rows = D == 3 ? tl.E[0] * tl.E[1] : tl.E[0];
-  for (int row = warp; row < rows; row += nwarps) {
-    int64_t gbase;
-    if (D == 3) {
-      const int p0 = row / tl.E[1], p1 = row - p0 * tl.E[1];
-      gbase = (wrap_pow2(o.a[0] + p0, geo.n[0]) * geo.n[1] + wrap_pow2(o.a[1] + p1, geo.n[1])) * geo.n[2];
-    } else {
-      gbase = wrap_pow2(o.a[0] + row, geo.n[0]) * geo.n[1];
-    }
-    const C* src = tile + (int64_t)row * tl.S;
-    for (int p = lane; p < E_last; p += kWarp) {
-      C v = src[p];
-      if (v.x != 0 || v.y != 0) global_add(&gi[gbase + wrap_pow2(o.a[D - 1] + p, n_last)], v);
-    }
-  }
-}
-
-template <int D, int W, typename T>
-__device__ __forceinline__ void compute_batch_weights(T* wb, const T* __restrict__ sfrac, int64_t first, int nb,
-                                                      const Geom& geo, int lane) {
-  const int q = lane / D, t = lane - q * D;
-  if (q < nb) {
-    const T fr = sfrac[(first + q) * D + t];
-    WeightMath<T>::taps(fr, geo.m, geo.b[t], W, wb + (q * D + t) * W);
+  const int total = rows * E_last;
+  for (int e = tid; e < total; e += nt) {
+    const int row = e / E_last, p = e - row * E_last;
+    const C v = tile[row * tl.S + p];
+    if (v.x != 0 || v.y != 0) global_add(gi + row_base<D>(geo, tl, o, row) + wrap_pow2(a_last + p, n_last), v);
   }
 }
 
@@ -184,90 +209,124 @@ __device__ __forceinline__ bool next_item(const Bins& bins, int slot, int4* cur)
   return cur->x >= 0;
 }
 
+// Shared-memory bytes beyond the tile, per kernel kind (the host sizes launches with it).
+__host__ __device__ constexpr int nodes_per_warp_batch(int d) { return d == 1 ? 32 : (d == 2 ? 8 : 5); }
+constexpr int kNodesPerCtaBatch = 32;
+
+__host__ __device__ inline size_t grid_extra_smem(int d, int W, size_t real, int nwarps, size_t tile_bytes,
+                                                  bool spread) {
+  if (!spread) {
+    const int nb = nodes_per_warp_batch(d);
+    return (size_t)nwarps * ((size_t)nb * d * W * real + (size_t)nb * 2 * sizeof(int));
+  }
+  const size_t batch = (size_t)kNodesPerCtaBatch * d * W * real + (size_t)kNodesPerCtaBatch * (sizeof(int) + 2 * real);
+  return d == 1 ? (size_t)(nwarps - 1) * tile_bytes + batch : batch;
+}
+
+template <int D, int W, typename T>
+struct GridSmem {
+  static constexpr int kNBW = nodes_per_warp_batch(D);  // nodes per warp batch (interpolation)
+  static constexpr int kNBC = kNodesPerCtaBatch;       // nodes per CTA batch (spreading)
+};
+
 // ---------------------------------------------------------------------------
-// d = 2, 3: warp per node
+// Interpolation, d = 1..3
 // ---------------------------------------------------------------------------
-template <int D, int W, typename T, bool SPREAD>
-__global__ void __launch_bounds__(512) k_grid(const typename Cx<T>::t* __restrict__ in,
-                                              typename Cx<T>::t* __restrict__ out,
-                                              Geom geo, Tiling tl, Bins bins) {
+template <int D, int W, typename T>
+__global__ void __launch_bounds__(512) k_interp(const typename Cx<T>::t* __restrict__ g,
+                                                typename Cx<T>::t* __restrict__ f, Geom geo, Tiling tl, Bins bins) {
   using C = typename Cx<T>::t;
-  static_assert(D == 2 || D == 3, "warp-per-node kernel is for d = 2, 3");
-  constexpr int R = kWarp / W;              // rows per warp pass
-  constexpr int NIT = (W + R - 1) / R;      // passes over the W rows of a plane
-  constexpr int NB = kWarp / D;             // nodes per weight batch
+  constexpr int R = kWarp / W;           // rows (d >= 2) or nodes (d = 1) per warp pass
+  constexpr int NIT = (W + R - 1) / R;   // passes over the W rows of a plane
+  constexpr int NB = GridSmem<D, W, T>::kNBW;
+  constexpr int SH = off_bits(D);
+  constexpr uint32_t MASK = (1u << SH) - 1u;
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ int4 cur;
   C* tile = reinterpret_cast<C*>(smem);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   T* wb = reinterpret_cast<T*>(smem + tl.smem_tile) + warp * (NB * D * W);
+  int* nrec = reinterpret_cast<int*>(reinterpret_cast<T*>(smem + tl.smem_tile) + nwarps * (NB * D * W)) + warp * 2 * NB;
   const int r = lane / W, l_last = lane - r * W;
   const bool lane_on = r < R;
   const int S = tl.S;
-  const int64_t PS = (int64_t)tl.R1 * S;    // plane stride (d = 3)
+  const int PS = tl.R1 * S;  // plane stride (d = 3)
   const T* sfrac = reinterpret_cast<const T*>(bins.sfrac);
   const T norm = (T)geo.norm;
 
-  while (next_item(bins, SPREAD ? 1 : 0, &cur)) {
+  while (next_item(bins, 0, &cur)) {
     const int4 item = cur;
-    const TileOrigin o = decode_tile(geo, tl, item.x);
-    if (SPREAD) {
-      const int rows = D == 3 ? tl.E[0] * tl.E[1] : tl.E[0];
-      C z;
-      z.x = (T)0;
-      z.y = (T)0;
-      for (int e = threadIdx.x; e < rows * S; e += blockDim.x) tile[e] = z;
-    } else {
-      load_tile<D, C>(tile, in + o.inst * geo.ntot, geo, tl, o, warp, nwarps, lane);
-    }
+    const TileOrigin o = decode_tile<D>(geo, tl, item.x);
+    load_tile<D, C>(tile, g + o.inst * geo.ntot, geo, tl, o);
     __syncthreads();
-
-    for (int64_t bs = item.y + (int64_t)warp * NB; bs < item.z; bs += (int64_t)nwarps * NB) {
-      const int nb = (int)min((int64_t)NB, item.z - bs);
-      compute_batch_weights<D, W, T>(wb, sfrac, bs, nb, geo, lane);
+    for (int bs = item.y + warp * NB; bs < item.z; bs += nwarps * NB) {
+      const int nb = min(NB, item.z - bs);
+      // stage the batch: records and tap weights (lane (q, t) computes psi_t of node q)
+      if (lane < nb) {
+        nrec[lane] = bins.sidx[bs + lane];
+        nrec[NB + lane] = bins.soff[bs + lane];
+      }
+      {
+        const int q = lane / D, t = lane - q * D;
+        if (q < nb) WeightMath<T>::taps(sfrac[(int64_t)(bs + q) * D + t], geo.m, geo_b(geo, t), W, wb + (q * D + t) * W);
+      }
       __syncwarp();
-      for (int q = 0; q < nb; ++q) {
-        const int64_t k = bs + q;
-        const int idx = bins.sidx[k];
-        const uint32_t off = (uint32_t)bins.soff[k];
-        const T* wq = wb + q * D * W;
-        const T w_last = wq[(D - 1) * W + (lane_on ? l_last : 0)];
-        T wrow[NIT];
+      if (D == 1) {
+        for (int q0 = 0; q0 < nb; q0 += R) {
+          const int q = q0 + r;
+          const bool on = lane_on && q < nb;
+          const int qq = on ? q : q0;
+          const int o0 = nrec[NB + qq] & MASK;
+          C acc = on ? cscale(tile[o0 + l_last], wb[qq * W + l_last]) : czero<C>();
 #pragma unroll
-        for (int it = 0; it < NIT; ++it) {
-          const int lr = r + it * R;
-          wrow[it] = (lane_on && lr < W) ? wq[(D - 2) * W + lr] : (T)0;
+          for (int s = 1; s < W; s <<= 1) {
+            C o2;
+            o2.x = __shfl_down_sync(0xffffffffu, acc.x, s);
+            o2.y = __shfl_down_sync(0xffffffffu, acc.y, s);
+            if (l_last + s < W) {
+              acc.x += o2.x;
+              acc.y += o2.y;
+            }
+          }
+          if (on && l_last == 0) f[nrec[qq]] = cscale(acc, norm);
         }
-        int64_t base;
-        if (D == 3) {
-          const int o0 = off & 1023, o1 = (off >> 10) & 1023, o2 = off >> 20;
-          base = o0 * PS + (int64_t)(o1 + r) * S + o2 + l_last;
-        } else {
-          const int o0 = off & 1023, o1 = (off >> 10) & 1023;
-          base = (int64_t)(o0 + r) * S + o1 + l_last;
-        }
-        T wpl[D == 3 ? W : 1];  // plane weights (d = 3), held in registers
-        if (D == 3) {
+      } else {
+        for (int q = 0; q < nb; ++q) {
+          const uint32_t off = (uint32_t)nrec[NB + q];
+          const T* wq = wb + q * D * W;
+          const T w_last = wq[(D - 1) * W + (lane_on ? l_last : 0)];
+          T wrow[NIT];
 #pragma unroll
-          for (int l0 = 0; l0 < W; ++l0) wpl[l0] = wq[l0];
-        }
-        if (!SPREAD) {
-          C acc;
-          acc.x = (T)0;
-          acc.y = (T)0;
+          for (int it = 0; it < NIT; ++it) {
+            const int lr = r + it * R;
+            wrow[it] = (lane_on && lr < W) ? wq[(D - 2) * W + lr] : (T)0;
+          }
+          T wpl[D == 3 ? W : 1];
+          if (D == 3) {
+#pragma unroll
+            for (int l0 = 0; l0 < W; ++l0) wpl[l0] = wq[l0];
+          }
+          int base;
+          if (D == 3) {
+            const int o0 = off & MASK, o1 = (off >> SH) & MASK, o2 = off >> (2 * SH);
+            base = o0 * PS + (o1 + r) * S + o2 + l_last;
+          } else {
+            const int o0 = off & MASK, o1 = (off >> SH) & MASK;
+            base = (o0 + r) * S + o1 + l_last;
+          }
+          C acc = czero<C>();
           if (lane_on) {
 #pragma unroll
             for (int it = 0; it < NIT; ++it) {
               if (r + it * R < W) {
-                const C* row = tile + base + (int64_t)it * R * S;
+                const int rb = base + it * R * S;
                 C ra;
                 if (D == 3) {
-                  ra.x = (T)0;
-                  ra.y = (T)0;
+                  ra = czero<C>();
 #pragma unroll
-                  for (int l0 = 0; l0 < W; ++l0) ra = cmul_add(ra, wpl[l0], row[l0 * PS]);
+                  for (int l0 = 0; l0 < W; ++l0) ra = cmul_add(ra, wpl[l0], tile[rb + l0 * PS]);
                 } else {
-                  ra = row[0];
+                  ra = tile[rb];
                 }
                 acc = cmul_add(acc, wrow[it], ra);
               }
@@ -276,115 +335,148 @@ __global__ void __launch_bounds__(512) k_grid(const typename Cx<T>::t* __restric
           }
 #pragma unroll
           for (int s = 16; s >= 1; s >>= 1) {
-            C o2 = shfl_xor_c<C>(acc, s);
+            const C o2 = shfl_xor_c<C>(acc, s);
             acc.x += o2.x;
             acc.y += o2.y;
           }
-          if (lane == 0) out[idx] = cscale(acc, norm);
-        } else {
-          const C v = cscale(in[idx], norm * w_last);
-          if (lane_on) {
+          if (lane == 0) f[nrec[q]] = cscale(acc, norm);
+        }
+      }
+      __syncwarp();
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Spreading, d = 1..3
+// ---------------------------------------------------------------------------
+template <int D, int W, typename T>
+__global__ void __launch_bounds__(512) k_spread(const typename Cx<T>::t* __restrict__ f,
+                                                typename Cx<T>::t* __restrict__ g, Geom geo, Tiling tl, Bins bins) {
+  using C = typename Cx<T>::t;
+  constexpr int R = kWarp / W;
+  constexpr int NIT = (W + R - 1) / R;
+  constexpr int NBC = GridSmem<D, W, T>::kNBC;
+  constexpr int SH = off_bits(D);
+  constexpr uint32_t MASK = (1u << SH) - 1u;
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ int4 cur;
+  C* tile = reinterpret_cast<C*>(smem);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int tile_elems = tile_rows<D>(tl) * tl.S;
+  // d = 1: one private tile copy per warp (copy 0 is `tile`)
+  const size_t extra = D == 1 ? (size_t)(nwarps - 1) * tl.smem_tile : 0;
+  unsigned char* bptr = smem + tl.smem_tile + extra;
+  T* cw = reinterpret_cast<T*>(bptr);                                      // [NBC][D][W]
+  C* cval = reinterpret_cast<C*>(cw + NBC * D * W);                        // [NBC]
+  int* coff = reinterpret_cast<int*>(cval + NBC);                          // [NBC]
+  const int r = lane / W, l_last = lane - r * W;
+  const bool lane_on = r < R;
+  const int S = tl.S;
+  const int PS = tl.R1 * S;
+  const T* sfrac = reinterpret_cast<const T*>(bins.sfrac);
+  const T norm = (T)geo.norm;
+  C* mytile = D == 1 ? reinterpret_cast<C*>(smem + (warp == 0 ? 0 : tl.smem_tile + (size_t)(warp - 1) * tl.smem_tile))
+                     : tile;
+
+  while (next_item(bins, 1, &cur)) {
+    const int4 item = cur;
+    const TileOrigin o = decode_tile<D>(geo, tl, item.x);
+    {
+      const C z = czero<C>();
+      if (D == 1) {
+        for (int e = lane; e < tile_elems; e += kWarp) mytile[e] = z;
+      } else {
+        for (int e = threadIdx.x; e < tile_elems; e += blockDim.x) tile[e] = z;
+      }
+    }
+    for (int bs = item.y; bs < item.z; bs += NBC) {
+      const int nb = min(NBC, item.z - bs);
+      __syncthreads();  // previous batch consumed (and the tile cleared)
+      for (int e = threadIdx.x; e < nb * D; e += blockDim.x) {
+        const int q = e / D, t = e - q * D;
+        WeightMath<T>::taps(sfrac[(int64_t)(bs + q) * D + t], geo.m, geo_b(geo, t), W, cw + (q * D + t) * W);
+      }
+      for (int q = threadIdx.x; q < nb; q += blockDim.x) {
+        coff[q] = bins.soff[bs + q];
+        cval[q] = cscale(f[bins.sidx[bs + q]], norm);
+      }
+      __syncthreads();
+      if (D == 1) {
+        // warp w takes nodes w, w + nwarps, ...; lanes are the node's taps
+        for (int q = warp; q < nb; q += nwarps) {
+          const int o0 = coff[q] & MASK;
+          if (lane < W) {
+            C* p = mytile + o0 + lane;
+            *p = cmul_add(*p, cw[q * W + lane], cval[q]);
+          }
+        }
+      } else if (D == 2) {
+        // warp w owns the row groups {g : g % nwarps == w}, group g = rows g*R .. g*R+R-1
+        for (int q = 0; q < nb; ++q) {
+          const uint32_t off = (uint32_t)coff[q];
+          const int o0 = off & MASK, o1 = (off >> SH) & MASK;
+          const int g_first = o0 / R, g_last = (o0 + W - 1) / R;
+          int g0 = g_first + ((warp - g_first % nwarps) + nwarps) % nwarps;
+          if (g0 > g_last || !lane_on) continue;
+          const T* wq = cw + q * 2 * W;
+          const C v = cscale(cval[q], wq[W + l_last]);
+          for (int gg = g0; gg <= g_last; gg += nwarps) {
+            const int p0 = gg * R + r;
+            if (p0 >= o0 && p0 < o0 + W) {
+              C* p = tile + p0 * S + o1 + l_last;
+              *p = cmul_add(*p, wq[p0 - o0], v);
+            }
+          }
+        }
+      } else {
+        // warp w owns the planes {p : p % nwarps == w}
+        for (int q = 0; q < nb; ++q) {
+          const uint32_t off = (uint32_t)coff[q];
+          const int o0 = off & MASK, o1 = (off >> SH) & MASK, o2 = off >> (2 * SH);
+          int p = o0 + ((warp - o0 % nwarps) + nwarps) % nwarps;
+          if (p >= o0 + W || !lane_on) continue;
+          const T* wq = cw + q * 3 * W;
+          const C v = cscale(cval[q], wq[2 * W + l_last]);
+          C vr[NIT];
+#pragma unroll
+          for (int it = 0; it < NIT; ++it) {
+            const int l1 = r + it * R;
+            vr[it] = cscale(v, l1 < W ? wq[W + l1] : (T)0);
+          }
+          const int cbase = (o1 + r) * S + o2 + l_last;
+          for (; p < o0 + W; p += nwarps) {
+            const T w0 = wq[p - o0];
+            const int pb = p * PS + cbase;
 #pragma unroll
             for (int it = 0; it < NIT; ++it) {
               if (r + it * R < W) {
-                C* row = tile + base + (int64_t)it * R * S;
-                const C vr = cscale(v, wrow[it]);
-                if (D == 3) {
-#pragma unroll
-                  for (int l0 = 0; l0 < W; ++l0) {
-                    const C t = cscale(vr, wpl[l0]);
-                    atomicAdd(&row[l0 * PS].x, t.x);
-                    atomicAdd(&row[l0 * PS].y, t.y);
-                  }
-                } else {
-                  atomicAdd(&row[0].x, vr.x);
-                  atomicAdd(&row[0].y, vr.y);
-                }
+                C* t = tile + pb + it * R * S;
+                *t = cmul_add(*t, w0, vr[it]);
               }
             }
           }
         }
       }
-      __syncwarp();
     }
     __syncthreads();
-    if (SPREAD) {
-      flush_tile<D, C>(tile, out + o.inst * geo.ntot, geo, tl, o, warp, nwarps, lane);
-      __syncthreads();
-    }
-  }
-}
-
-// ---------------------------------------------------------------------------
-// d = 1: R = 32/W nodes per warp pass, lane (node r, tap l)
-// ---------------------------------------------------------------------------
-template <int W, typename T, bool SPREAD>
-__global__ void __launch_bounds__(512) k_grid1(const typename Cx<T>::t* __restrict__ in,
-                                               typename Cx<T>::t* __restrict__ out,
-                                               Geom geo, Tiling tl, Bins bins) {
-  using C = typename Cx<T>::t;
-  constexpr int R = kWarp / W;
-  constexpr int NB = kWarp;   // weights of 32 nodes per batch (one lane each)
-  extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ int4 cur;
-  C* tile = reinterpret_cast<C*>(smem);
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  T* wb = reinterpret_cast<T*>(smem + tl.smem_tile) + warp * (NB * W);
-  const int r = lane / W, l = lane - r * W;
-  const bool lane_on = r < R;
-  const T* sfrac = reinterpret_cast<const T*>(bins.sfrac);
-  const T norm = (T)geo.norm;
-
-  while (next_item(bins, SPREAD ? 1 : 0, &cur)) {
-    const int4 item = cur;
-    const TileOrigin o = decode_tile(geo, tl, item.x);
-    if (SPREAD) {
-      C z;
-      z.x = (T)0;
-      z.y = (T)0;
-      for (int e = threadIdx.x; e < tl.S; e += blockDim.x) tile[e] = z;
-    } else {
-      load_tile<1, C>(tile, in + o.inst * geo.ntot, geo, tl, o, warp, nwarps, lane);
-    }
-    __syncthreads();
-    for (int64_t bs = item.y + (int64_t)warp * NB; bs < item.z; bs += (int64_t)nwarps * NB) {
-      const int nb = (int)min((int64_t)NB, item.z - bs);
-      compute_batch_weights<1, W, T>(wb, sfrac, bs, nb, geo, lane);
-      __syncwarp();
-      for (int q0 = 0; q0 < nb; q0 += R) {
-        const int q = q0 + r;
-        const bool on = lane_on && q < nb;
-        const int64_t k = bs + (on ? q : q0);
-        const int idx = bins.sidx[k];
-        const int o0 = bins.soff[k] & 1023;
-        const T w = on ? wb[q * W + l] : (T)0;
-        if (!SPREAD) {
-          C acc = on ? cscale(tile[o0 + l], w) : C{(T)0, (T)0};
-          // segmented reduction over the W lanes of node r
-#pragma unroll
-          for (int s = 1; s < W; s <<= 1) {
-            C o2;
-            o2.x = __shfl_down_sync(0xffffffffu, acc.x, s);
-            o2.y = __shfl_down_sync(0xffffffffu, acc.y, s);
-            if (l + s < W) {
-              acc.x += o2.x;
-              acc.y += o2.y;
-            }
-          }
-          if (on && l == 0) out[idx] = cscale(acc, norm);
-        } else if (on) {
-          const C v = cscale(in[idx], norm * w);
-          atomicAdd(&tile[o0 + l].x, v.x);
-          atomicAdd(&tile[o0 + l].y, v.y);
+    if (D == 1) {
+      // fold the private copies into copy 0, then flush
+      const int nw = nwarps;
+      for (int e = threadIdx.x; e < tile_elems; e += blockDim.x) {
+        C s = tile[e];
+        for (int w = 1; w < nw; ++w) {
+          const C v = reinterpret_cast<C*>(smem + tl.smem_tile + (size_t)(w - 1) * tl.smem_tile)[e];
+          s.x += v.x;
+          s.y += v.y;
         }
+        tile[e] = s;
       }
-      __syncwarp();
-    }
-    __syncthreads();
-    if (SPREAD) {
-      flush_tile<1, C>(tile, out + o.inst * geo.ntot, geo, tl, o, warp, nwarps, lane);
       __syncthreads();
     }
+    flush_tile<D, C>(tile, g + o.inst * geo.ntot, geo, tl, o);
+    __syncthreads();
   }
 }
 

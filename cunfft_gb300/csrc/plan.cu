@@ -86,18 +86,8 @@ static void default_tiles(const Plan* p, int* T) {
   }
 }
 
-int plan_choose_tiling(Plan* p, const int* Tin, int chunk) {
+static Tiling make_tiling(const Plan* p, const int* T, int chunk) {
   const int d = p->geo.d, W = p->geo.W;
-  int T[kMaxDim] = {1, 1, 1};
-  default_tiles(p, T);
-  for (int t = 0; t < d; ++t) {
-    if (Tin && Tin[t] > 0) {
-      if (!is_pow2(Tin[t]) || Tin[t] > 1024)
-        return set_status(p, CUNFFT_X_INVALID_ARGUMENT, "tile extent %d is not a power of two <= 1024", Tin[t]);
-      T[t] = Tin[t];
-    }
-    if (T[t] > p->geo.n[t]) T[t] = (int)p->geo.n[t];
-  }
   Tiling tl{};
   for (int t = 0; t < kMaxDim; ++t) {
     tl.T[t] = t < d ? T[t] : 1;
@@ -120,17 +110,51 @@ int plan_choose_tiling(Plan* p, const int* Tin, int chunk) {
   tl.tiles_total = tl.tiles_per_inst * p->geo.batch;
   tl.threads = 256;
   tl.chunk = chunk > 0 ? chunk : (d == 3 ? 1024 : 2048);
-  Tiling old = p->tl;
+  tl.use_global = 0;
+  return tl;
+}
+
+static size_t smem_of(const Plan* p, const Tiling& tl) {
+  Plan q = *p;  // shallow copy for the size computation only
+  q.tl = tl;
+  return gridding_smem_bytes(q);
+}
+
+// Tile extents: the caller's (or the defaults), clamped to the grid.  When the
+// padded tile does not fit in shared memory the largest extent is halved until it
+// does; when even 1-cell tiles do not fit (wide windows in 3D), the gridding runs
+// on the global-memory kernels with the default tiles as work items.
+int plan_choose_tiling(Plan* p, const int* Tin, int chunk) {
+  const int d = p->geo.d;
+  const size_t kMaxSmem = 227 * 1024;
+  int T[kMaxDim] = {1, 1, 1};
+  default_tiles(p, T);
+  for (int t = 0; t < d; ++t) {
+    if (Tin && Tin[t] > 0) {
+      const int tmax = d == 3 ? 1024 : (d == 2 ? 32768 : (1 << 30));  // packed offset: 30/d bits per dim
+      if (!is_pow2(Tin[t]) || Tin[t] > tmax)
+        return set_status(p, CUNFFT_X_INVALID_ARGUMENT, "tile extent %d is not a power of two <= %d", Tin[t], tmax);
+      T[t] = Tin[t];
+    }
+    if (T[t] > p->geo.n[t]) T[t] = (int)p->geo.n[t];
+  }
+  int Tfit[kMaxDim] = {T[0], T[1], T[2]};
+  Tiling tl = make_tiling(p, Tfit, chunk);
+  while (smem_of(p, tl) > kMaxSmem) {
+    int big = 0;
+    for (int t = 1; t < d; ++t)
+      if (Tfit[t] > Tfit[big]) big = t;
+    if (Tfit[big] == 1) break;
+    Tfit[big] /= 2;
+    tl = make_tiling(p, Tfit, chunk);
+  }
+  if (smem_of(p, tl) > kMaxSmem) {
+    tl = make_tiling(p, T, chunk);
+    tl.use_global = 1;
+    tl.threads = 128;
+  }
+  if (tl.tiles_total >= (int64_t)1 << 31) return set_status(p, CUNFFT_X_INVALID_ARGUMENT, "too many tiles");
   p->tl = tl;
-  if (gridding_smem_bytes(*p) > 227 * 1024) {
-    p->tl = old;
-    return set_status(p, CUNFFT_X_INVALID_ARGUMENT, "tile needs %zu bytes of shared memory (max 227 KB)",
-                      gridding_smem_bytes(*p));
-  }
-  if (tl.tiles_total >= (int64_t)1 << 31) {
-    p->tl = old;
-    return set_status(p, CUNFFT_X_INVALID_ARGUMENT, "too many tiles");
-  }
   p->bins.valid = 0;
   return CUNFFT_X_SUCCESS;
 }
