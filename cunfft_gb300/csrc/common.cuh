@@ -34,7 +34,26 @@ struct Geom {
   int64_t Ntot, ntot;    // per instance
   double b[kMaxDim];     // Gaussian shape parameter per dim
   double norm;           // prod_t sqrt(b'_t), b' = (2 sigma-1)/(2 sigma m) = 1/(pi b)
+  float cbf[kMaxDim];    // log2(e) / b_t, rounded to FP32 (FP32 tap weights exp2(-y^2 cb))
 };
+
+// Compile-time extents of the inner tile dimensions of the shared-memory
+// gridding kernels (the outermost extent T0 stays a runtime, tunable value):
+// d = 3: T1 x T2 = 8 x 16 (4 x 8 for windows wider than 16 taps); d = 2: T1 = 64.
+// With them the row stride S and plane stride PS are constants, so every tap's
+// shared-memory offset is an immediate.
+__host__ __device__ constexpr int fixed_t_last(int d, int W) { return d == 3 ? (W <= 16 ? 16 : 8) : (d == 2 ? 64 : 1); }
+__host__ __device__ constexpr int fixed_t_mid(int d, int W) { return d == 3 ? (W <= 16 ? 8 : 4) : 1; }
+// smallest S >= E with S == W (mod 16): lane i of the (row, tap) mapping lands in bank group i
+__host__ __device__ constexpr int conflict_free_stride(int E, int W) {
+  return E + ((((W - E) % 16) + 16) % 16);
+}
+__host__ __device__ constexpr int fixed_row_stride(int d, int W) {
+  return d == 1 ? 0 : conflict_free_stride(fixed_t_last(d, W) + W - 1, W);
+}
+__host__ __device__ constexpr int fixed_plane_stride(int d, int W) {
+  return d == 3 ? (fixed_t_mid(d, W) + W - 1) * fixed_row_stride(d, W) : fixed_row_stride(d, W);
+}
 
 // Tiling of the oversampled grid used by the gridding kernels.
 struct Tiling {

@@ -10,21 +10,24 @@
 //    atomic queue, so clustered node sets (thousands of nodes in one tile) spread
 //    over many CTAs instead of serialising on one.
 //  * The CTA stages the padded tile (T_t + W - 1 per dim, wrapped mod n) in shared
-//    memory.  Row stride S == W (mod 16) elements, so the lane -> tap mapping below
-//    touches consecutive shared-memory banks: no bank conflicts for 8-byte
-//    (float2) or 16-byte (double2) elements.  All shared-memory indices are 32-bit.
+//    memory.  The inner strides are compile-time constants (common.cuh): row
+//    stride S == W (mod 16) elements, so the lane -> tap mapping below touches
+//    consecutive banks (no conflicts for float2 or double2 elements), and every
+//    tap offset is an immediate.
 //  * Lane i < R*W (R = 32/W) owns innermost tap l_last = i % W and rows
 //    r = i / W, r + R, ... of the remaining taps (for d = 3 a row is an (l0, l1)
 //    pair walked over the 2m+2 planes l0).
 //  * Interpolation: one warp per node at a time; the warp reduces the node's sum
 //    with shuffles.  Node records and tap weights of a batch of nodes are staged
-//    per warp in shared memory, so the tap loop does no global loads.
+//    per warp in shared memory; the next batch's records are fetched into
+//    registers while the current batch runs.
 //  * Spreading: no shared-memory atomics (a float atomic add on shared memory is a
 //    compare-and-swap loop).  Every warp walks all nodes of a CTA-wide batch but
 //    writes only the planes (d = 3) or row groups (d = 2) it owns, with plain
 //    load / FMA / store; for d = 1 each warp accumulates into a private copy of
-//    the tile.  The tile is then added to the global grid with vector atomics, so
-//    neighbouring items' halos combine.
+//    the tile.  Batches are double-buffered (one barrier per batch).  The tile is
+//    then added to the global grid with vector atomics, so neighbouring items'
+//    halos combine.
 //  * Tap weights: exp2f per tap in the FP32 form; in the FP64 form the reference's
 //    fast-Gaussian-gridding recurrence (2 exp per node and dim, src/cunfft_kernel.cu:
 //    491-505), which keeps the scarce FP64 pipe on the taps.
@@ -41,8 +44,8 @@ template <typename T> struct WeightMath;
 
 template <> struct WeightMath<float> {
   // psi(l) / sqrt(b') = exp(-(fr + m - l)^2 / b) = exp2(-(y*y) * log2(e)/b)
-  static __device__ __forceinline__ void taps(float fr, int m, double b, int W, float* out) {
-    const float cb = (float)(1.4426950408889634 / b);
+  static __device__ __forceinline__ void taps(float fr, int m, const Geom& g, int t, int W, float* out) {
+    const float cb = t == 0 ? g.cbf[0] : (t == 1 ? g.cbf[1] : g.cbf[2]);
 #pragma unroll 4
     for (int l = 0; l < W; ++l) {
       const float y = fr + (float)(m - l);
@@ -53,7 +56,8 @@ template <> struct WeightMath<float> {
 
 template <> struct WeightMath<double> {
   // FGG form: psi_l = phi * E^l * exp(-l^2/b), phi = exp(-c^2/b), E = exp(2c/b), c = m + fr.
-  static __device__ __forceinline__ void taps(double fr, int m, double b, int W, double* out) {
+  static __device__ __forceinline__ void taps(double fr, int m, const Geom& g, int t, int W, double* out) {
+    const double b = t == 0 ? g.b[0] : (t == 1 ? g.b[1] : g.b[2]);
     const double c = (double)m + fr;
     const double ib = 1.0 / b;
     const double phi = exp(-(c * c) * ib);
@@ -79,6 +83,35 @@ __device__ __forceinline__ double2 cmul_add(double2 acc, double w, double2 v) {
   acc.y = fma(w, v.y, acc.y);
   return acc;
 }
+// A weight ready for the complex multiply-add: the (w, w) pair of a packed
+// f32x2 FMA in the FP32 form, the scalar in the FP64 form.
+template <typename T> struct WPair;
+template <> struct WPair<float> {
+  using t = float2;
+  static __device__ __forceinline__ float2 make(float w) { return make_float2(w, w); }
+};
+template <> struct WPair<double> {
+  using t = double;
+  static __device__ __forceinline__ double make(double w) { return w; }
+};
+__device__ __forceinline__ float2 cmul_addp(float2 acc, float2 ww, float2 v) { return __ffma2_rn(ww, v, acc); }
+__device__ __forceinline__ double2 cmul_addp(double2 acc, double w, double2 v) {
+  acc.x = fma(w, v.x, acc.x);
+  acc.y = fma(w, v.y, acc.y);
+  return acc;
+}
+
+// Asynchronous global -> shared copy of one complex element (cp.async, 8 or 16 bytes).
+template <typename C>
+__device__ __forceinline__ void cp_async_elem(C* dst, const C* src) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
+  if constexpr (sizeof(C) == 16)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(src) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 __device__ __forceinline__ float2 cscale(float2 v, float w) { return __fmul2_rn(make_float2(w, w), v); }
 __device__ __forceinline__ double2 cscale(double2 v, double w) { return make_double2(v.x * w, v.y * w); }
 
@@ -102,8 +135,6 @@ __device__ __forceinline__ C shfl_xor_c(C v, int o) {
   v.y = __shfl_xor_sync(0xffffffffu, v.y, o);
   return v;
 }
-
-__device__ __forceinline__ double geo_b(const Geom& g, int t) { return t == 0 ? g.b[0] : (t == 1 ? g.b[1] : g.b[2]); }
 
 // Tile origin a_t of a work item's tile and its instance.
 struct TileOrigin {
@@ -130,72 +161,88 @@ __device__ __forceinline__ TileOrigin decode_tile(const Geom& geo, const Tiling&
 }
 
 // Rows of the staged tile: [E0][E1] for d = 3, [E0] for d = 2, one for d = 1.
+// The shared-memory row of (p0, p1) starts at p0 * PS + p1 * S.
 template <int D>
 __device__ __forceinline__ int tile_rows(const Tiling& tl) {
   return D == 3 ? tl.E[0] * tl.E[1] : (D == 2 ? tl.E[0] : 1);
 }
 
 template <int D>
-__device__ __forceinline__ int64_t row_base(const Geom& geo, const Tiling& tl, const TileOrigin& o, int row) {
+__device__ __forceinline__ void row_coords(const Tiling& tl, int row, int* p0, int* p1) {
   if (D == 3) {
-    const int p0 = row / tl.E[1], p1 = row - p0 * tl.E[1];
-    return (wrap_pow2(o.a[0] + p0, geo.n[0]) * geo.n[1] + wrap_pow2(o.a[1] + p1, geo.n[1])) * geo.n[2];
+    *p0 = row / tl.E[1];
+    *p1 = row - *p0 * tl.E[1];
+  } else {
+    *p0 = row;
+    *p1 = 0;
   }
-  if (D == 2) return wrap_pow2(o.a[0] + row, geo.n[0]) * geo.n[1];
+}
+
+template <int D>
+__device__ __forceinline__ int64_t row_gbase(const Geom& geo, const TileOrigin& o, int p0, int p1) {
+  if (D == 3) return (wrap_pow2(o.a[0] + p0, geo.n[0]) * geo.n[1] + wrap_pow2(o.a[1] + p1, geo.n[1])) * geo.n[2];
+  if (D == 2) return wrap_pow2(o.a[0] + p0, geo.n[0]) * geo.n[1];
   return 0;
 }
 
-template <int D, typename C>
+template <int D, int W, typename C>
 __device__ __forceinline__ void load_tile(C* tile, const C* __restrict__ gi, const Geom& geo, const Tiling& tl,
                                           const TileOrigin& o) {
+  constexpr int S = fixed_row_stride(D, W), PS = fixed_plane_stride(D, W);
   const int E_last = tl.E[D - 1];
   const int64_t n_last = geo.n[D - 1], a_last = o.a[D - 1];
   if (D == 1) {
-    for (int p = threadIdx.x; p < E_last; p += blockDim.x) tile[p] = gi[wrap_pow2(a_last + p, n_last)];
+    for (int p = threadIdx.x; p < E_last; p += blockDim.x) cp_async_elem(tile + p, gi + wrap_pow2(a_last + p, n_last));
+    cp_async_wait_all();
     return;
   }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const int rows = tile_rows<D>(tl);
   for (int row = warp; row < rows; row += nwarps) {
-    const int64_t gbase = row_base<D>(geo, tl, o, row);
-    C* dst = tile + row * tl.S;
-    for (int p = lane; p < E_last; p += kWarp) dst[p] = gi[gbase + wrap_pow2(a_last + p, n_last)];
+    int p0, p1;
+    row_coords<D>(tl, row, &p0, &p1);
+    const int64_t gbase = row_gbase<D>(geo, o, p0, p1);
+    C* dst = tile + (D == 3 ? p0 * PS + p1 * S : p0 * S);
+    for (int p = lane; p < E_last; p += kWarp) cp_async_elem(dst + p, gi + gbase + wrap_pow2(a_last + p, n_last));
   }
+  cp_async_wait_all();  // this thread's copies landed; the caller's barrier publishes them
 }
 
 // Add the tile into the global grid.  FP32 pairs (even offset, so 16-byte
 // aligned and never split by the power-of-two wrap) go as one float4 atomic.
-template <int D, typename C>
+template <int D, int W, typename C>
 __device__ __forceinline__ void flush_tile(const C* tile, C* __restrict__ gi, const Geom& geo, const Tiling& tl,
                                            const TileOrigin& o) {
+  constexpr int S = fixed_row_stride(D, W), PS = fixed_plane_stride(D, W);
   const int E_last = tl.E[D - 1];
   const int64_t n_last = geo.n[D - 1], a_last = o.a[D - 1];
   const int rows = tile_rows<D>(tl);
   constexpr bool kF32 = sizeof(C) == 8;
   const int tid = threadIdx.x, nt = blockDim.x;
-  if (kF32 && n_last >= 2 && (tl.T[D - 1] & 1) == 0) {  // even tile origin: pairs stay 16-byte aligned
-    const int pairs = (E_last + 1) >> 1;
-    const int total = rows * pairs;
-    for (int e = tid; e < total; e += nt) {
-      const int row = e / pairs, pp = e - row * pairs, p = 2 * pp;
-      const C* src = tile + row * tl.S + p;
-      const int64_t gidx = row_base<D>(geo, tl, o, row) + wrap_pow2(a_last + p, n_last);
-      const C v0 = src[0];
+  const bool pairs_ok = kF32 && n_last >= 2 && (tl.T[D - 1] & 1) == 0;  // even tile origin
+  const int per_row = pairs_ok ? (E_last + 1) >> 1 : E_last;
+  const int total = rows * per_row;
+  for (int e = tid; e < total; e += nt) {
+    const int row = e / per_row, k = e - row * per_row;
+    int p0, p1;
+    row_coords<D>(tl, row, &p0, &p1);
+    const C* src = tile + (D == 3 ? p0 * PS + p1 * S : (D == 2 ? p0 * S : 0));
+    const int64_t gb = row_gbase<D>(geo, o, p0, p1);
+    if (pairs_ok) {
+      const int p = 2 * k;
+      const C v0 = src[p];
+      const int64_t gidx = gb + wrap_pow2(a_last + p, n_last);
       if (p + 1 < E_last) {
-        const C v1 = src[1];
+        const C v1 = src[p + 1];
         if (v0.x != 0 || v0.y != 0 || v1.x != 0 || v1.y != 0)
           atomicAdd(reinterpret_cast<float4*>(gi + gidx), make_float4(v0.x, v0.y, v1.x, v1.y));
       } else if (v0.x != 0 || v0.y != 0) {
         global_add(gi + gidx, v0);
       }
+    } else {
+      const C v = src[k];
+      if (v.x != 0 || v.y != 0) global_add(gi + gb + wrap_pow2(a_last + k, n_last), v);
     }
-    return;
-  }
-  const int total = rows * E_last;
-  for (int e = tid; e < total; e += nt) {
-    const int row = e / E_last, p = e - row * E_last;
-    const C v = tile[row * tl.S + p];
-    if (v.x != 0 || v.y != 0) global_add(gi + row_base<D>(geo, tl, o, row) + wrap_pow2(a_last + p, n_last), v);
   }
 }
 
@@ -211,7 +258,7 @@ __device__ __forceinline__ bool next_item(const Bins& bins, int slot, int4* cur)
 
 // Shared-memory bytes beyond the tile, per kernel kind (the host sizes launches with it).
 __host__ __device__ constexpr int nodes_per_warp_batch(int d) { return d == 1 ? 32 : (d == 2 ? 8 : 5); }
-constexpr int kNodesPerCtaBatch = 32;
+constexpr int kNodesPerCtaBatch = 16;
 
 __host__ __device__ inline size_t grid_extra_smem(int d, int W, size_t real, int nwarps, size_t tile_bytes,
                                                   bool spread) {
@@ -219,15 +266,10 @@ __host__ __device__ inline size_t grid_extra_smem(int d, int W, size_t real, int
     const int nb = nodes_per_warp_batch(d);
     return (size_t)nwarps * ((size_t)nb * d * W * real + (size_t)nb * 2 * sizeof(int));
   }
+  // two batch buffers: weights, values, offsets
   const size_t batch = (size_t)kNodesPerCtaBatch * d * W * real + (size_t)kNodesPerCtaBatch * (sizeof(int) + 2 * real);
-  return d == 1 ? (size_t)(nwarps - 1) * tile_bytes + batch : batch;
+  return (d == 1 ? (size_t)(nwarps - 1) * tile_bytes : 0) + 2 * batch;
 }
-
-template <int D, int W, typename T>
-struct GridSmem {
-  static constexpr int kNBW = nodes_per_warp_batch(D);  // nodes per warp batch (interpolation)
-  static constexpr int kNBC = kNodesPerCtaBatch;       // nodes per CTA batch (spreading)
-};
 
 // ---------------------------------------------------------------------------
 // Interpolation, d = 1..3
@@ -238,9 +280,11 @@ __global__ void __launch_bounds__(512) k_interp(const typename Cx<T>::t* __restr
   using C = typename Cx<T>::t;
   constexpr int R = kWarp / W;           // rows (d >= 2) or nodes (d = 1) per warp pass
   constexpr int NIT = (W + R - 1) / R;   // passes over the W rows of a plane
-  constexpr int NB = GridSmem<D, W, T>::kNBW;
+  constexpr bool FULL = R * NIT == W;    // every lane's every pass is a real row
+  constexpr int NB = nodes_per_warp_batch(D);
   constexpr int SH = off_bits(D);
   constexpr uint32_t MASK = (1u << SH) - 1u;
+  constexpr int S = fixed_row_stride(D, W), PS = fixed_plane_stride(D, W);
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ int4 cur;
   C* tile = reinterpret_cast<C*>(smem);
@@ -249,26 +293,43 @@ __global__ void __launch_bounds__(512) k_interp(const typename Cx<T>::t* __restr
   int* nrec = reinterpret_cast<int*>(reinterpret_cast<T*>(smem + tl.smem_tile) + nwarps * (NB * D * W)) + warp * 2 * NB;
   const int r = lane / W, l_last = lane - r * W;
   const bool lane_on = r < R;
-  const int S = tl.S;
-  const int PS = tl.R1 * S;  // plane stride (d = 3)
   const T* sfrac = reinterpret_cast<const T*>(bins.sfrac);
   const T norm = (T)geo.norm;
+  const int qd = lane / D, td = lane - qd * D;  // (node, dim) of this lane in the weight pass
 
   while (next_item(bins, 0, &cur)) {
     const int4 item = cur;
     const TileOrigin o = decode_tile<D>(geo, tl, item.x);
-    load_tile<D, C>(tile, g + o.inst * geo.ntot, geo, tl, o);
-    __syncthreads();
-    for (int bs = item.y + warp * NB; bs < item.z; bs += nwarps * NB) {
-      const int nb = min(NB, item.z - bs);
-      // stage the batch: records and tap weights (lane (q, t) computes psi_t of node q)
-      if (lane < nb) {
-        nrec[lane] = bins.sidx[bs + lane];
-        nrec[NB + lane] = bins.soff[bs + lane];
+    load_tile<D, W, C>(tile, g + o.inst * geo.ntot, geo, tl, o);
+    // records of this warp's first batch
+    int bs = item.y + warp * NB;
+    int pf_idx = 0, pf_off = 0;
+    T pf_fr = 0;
+    if (bs < item.z) {
+      const int nb0 = min(NB, item.z - bs);
+      if (lane < nb0) {
+        pf_idx = bins.sidx[bs + lane];
+        pf_off = bins.soff[bs + lane];
       }
-      {
-        const int q = lane / D, t = lane - q * D;
-        if (q < nb) WeightMath<T>::taps(sfrac[(int64_t)(bs + q) * D + t], geo.m, geo_b(geo, t), W, wb + (q * D + t) * W);
+      if (qd < nb0) pf_fr = sfrac[(int64_t)(bs + qd) * D + td];
+    }
+    __syncthreads();
+    for (; bs < item.z; bs += nwarps * NB) {
+      const int nb = min(NB, item.z - bs);
+      if (lane < nb) {
+        nrec[lane] = pf_idx;
+        nrec[NB + lane] = pf_off;
+      }
+      if (qd < nb) WeightMath<T>::taps(pf_fr, geo.m, geo, td, W, wb + (qd * D + td) * W);
+      // fetch the next batch's records while this batch runs
+      const int bn = bs + nwarps * NB;
+      if (bn < item.z) {
+        const int nbn = min(NB, item.z - bn);
+        if (lane < nbn) {
+          pf_idx = bins.sidx[bn + lane];
+          pf_off = bins.soff[bn + lane];
+        }
+        if (qd < nbn) pf_fr = sfrac[(int64_t)(bn + qd) * D + td];
       }
       __syncwarp();
       if (D == 1) {
@@ -299,16 +360,16 @@ __global__ void __launch_bounds__(512) k_interp(const typename Cx<T>::t* __restr
 #pragma unroll
           for (int it = 0; it < NIT; ++it) {
             const int lr = r + it * R;
-            wrow[it] = (lane_on && lr < W) ? wq[(D - 2) * W + lr] : (T)0;
+            wrow[it] = (FULL || lr < W) ? wq[(D - 2) * W + (FULL ? lr : min(lr, W - 1))] : (T)0;
           }
-          T wpl[D == 3 ? W : 1];
+          typename WPair<T>::t wpl[D == 3 ? W : 1];
           if (D == 3) {
 #pragma unroll
-            for (int l0 = 0; l0 < W; ++l0) wpl[l0] = wq[l0];
+            for (int l0 = 0; l0 < W; ++l0) wpl[l0] = WPair<T>::make(wq[l0]);
           }
           int base;
           if (D == 3) {
-            const int o0 = off & MASK, o1 = (off >> SH) & MASK, o2 = off >> (2 * SH);
+            const int o0 = off & MASK, o1 = (off >> SH) & MASK, o2 = off >> (D == 3 ? 2 * SH : 0);
             base = o0 * PS + (o1 + r) * S + o2 + l_last;
           } else {
             const int o0 = off & MASK, o1 = (off >> SH) & MASK;
@@ -316,17 +377,17 @@ __global__ void __launch_bounds__(512) k_interp(const typename Cx<T>::t* __restr
           }
           C acc = czero<C>();
           if (lane_on) {
+            const C* tb = tile + base;
 #pragma unroll
             for (int it = 0; it < NIT; ++it) {
-              if (r + it * R < W) {
-                const int rb = base + it * R * S;
+              if (FULL || r + it * R < W) {
                 C ra;
                 if (D == 3) {
                   ra = czero<C>();
 #pragma unroll
-                  for (int l0 = 0; l0 < W; ++l0) ra = cmul_add(ra, wpl[l0], tile[rb + l0 * PS]);
+                  for (int l0 = 0; l0 < W; ++l0) ra = cmul_addp(ra, wpl[l0], tb[it * R * S + l0 * PS]);
                 } else {
-                  ra = tile[rb];
+                  ra = tb[it * R * S];
                 }
                 acc = cmul_add(acc, wrow[it], ra);
               }
@@ -357,28 +418,27 @@ __global__ void __launch_bounds__(512) k_spread(const typename Cx<T>::t* __restr
   using C = typename Cx<T>::t;
   constexpr int R = kWarp / W;
   constexpr int NIT = (W + R - 1) / R;
-  constexpr int NBC = GridSmem<D, W, T>::kNBC;
+  constexpr bool FULL = R * NIT == W;
+  constexpr int NBC = kNodesPerCtaBatch;
   constexpr int SH = off_bits(D);
   constexpr uint32_t MASK = (1u << SH) - 1u;
+  constexpr int S = fixed_row_stride(D, W), PS = fixed_plane_stride(D, W);
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ int4 cur;
   C* tile = reinterpret_cast<C*>(smem);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  const int tile_elems = tile_rows<D>(tl) * tl.S;
+  const int tile_elems = D == 1 ? tl.E[0] : (D == 2 ? tl.E[0] * S : tl.E[0] * PS);
   // d = 1: one private tile copy per warp (copy 0 is `tile`)
   const size_t extra = D == 1 ? (size_t)(nwarps - 1) * tl.smem_tile : 0;
   unsigned char* bptr = smem + tl.smem_tile + extra;
-  T* cw = reinterpret_cast<T*>(bptr);                                      // [NBC][D][W]
-  C* cval = reinterpret_cast<C*>(cw + NBC * D * W);                        // [NBC]
-  int* coff = reinterpret_cast<int*>(cval + NBC);                          // [NBC]
+  const size_t batch_bytes = (size_t)NBC * D * W * sizeof(T) + (size_t)NBC * (sizeof(int) + sizeof(C));
   const int r = lane / W, l_last = lane - r * W;
   const bool lane_on = r < R;
-  const int S = tl.S;
-  const int PS = tl.R1 * S;
   const T* sfrac = reinterpret_cast<const T*>(bins.sfrac);
   const T norm = (T)geo.norm;
-  C* mytile = D == 1 ? reinterpret_cast<C*>(smem + (warp == 0 ? 0 : tl.smem_tile + (size_t)(warp - 1) * tl.smem_tile))
-                     : tile;
+  C* mytile = D == 1 ? reinterpret_cast<C*>(smem + (size_t)warp * tl.smem_tile) : tile;
+  // this thread's staging role: (node, dim) for weights, node for records
+  const int sq = threadIdx.x / D, st = threadIdx.x - sq * D;
 
   while (next_item(bins, 1, &cur)) {
     const int4 item = cur;
@@ -391,18 +451,41 @@ __global__ void __launch_bounds__(512) k_spread(const typename Cx<T>::t* __restr
         for (int e = threadIdx.x; e < tile_elems; e += blockDim.x) tile[e] = z;
       }
     }
-    for (int bs = item.y; bs < item.z; bs += NBC) {
+    // records of the first batch
+    T pf_fr = 0;
+    int pf_off = 0;
+    C pf_val = czero<C>();
+    {
+      const int nb0 = min(NBC, item.z - item.y);
+      if (sq < nb0) pf_fr = sfrac[(int64_t)(item.y + sq) * D + st];
+      if ((int)threadIdx.x < nb0) {
+        pf_off = bins.soff[item.y + threadIdx.x];
+        pf_val = f[bins.sidx[item.y + threadIdx.x]];
+      }
+    }
+    int buf = 0;
+    for (int bs = item.y; bs < item.z; bs += NBC, buf ^= 1) {
       const int nb = min(NBC, item.z - bs);
-      __syncthreads();  // previous batch consumed (and the tile cleared)
-      for (int e = threadIdx.x; e < nb * D; e += blockDim.x) {
-        const int q = e / D, t = e - q * D;
-        WeightMath<T>::taps(sfrac[(int64_t)(bs + q) * D + t], geo.m, geo_b(geo, t), W, cw + (q * D + t) * W);
+      unsigned char* bb = bptr + buf * batch_bytes;
+      T* cw = reinterpret_cast<T*>(bb);                      // [NBC][D][W]
+      C* cval = reinterpret_cast<C*>(cw + NBC * D * W);      // [NBC]
+      int* coff = reinterpret_cast<int*>(cval + NBC);        // [NBC]
+      if (sq < nb) WeightMath<T>::taps(pf_fr, geo.m, geo, st, W, cw + (sq * D + st) * W);
+      if ((int)threadIdx.x < nb) {
+        coff[threadIdx.x] = pf_off;
+        cval[threadIdx.x] = cscale(pf_val, norm);
       }
-      for (int q = threadIdx.x; q < nb; q += blockDim.x) {
-        coff[q] = bins.soff[bs + q];
-        cval[q] = cscale(f[bins.sidx[bs + q]], norm);
+      // fetch the next batch's records
+      const int bn = bs + NBC;
+      if (bn < item.z) {
+        const int nbn = min(NBC, item.z - bn);
+        if (sq < nbn) pf_fr = sfrac[(int64_t)(bn + sq) * D + st];
+        if ((int)threadIdx.x < nbn) {
+          pf_off = bins.soff[bn + threadIdx.x];
+          pf_val = f[bins.sidx[bn + threadIdx.x]];
+        }
       }
-      __syncthreads();
+      __syncthreads();  // batch staged (and, for the first batch, the tile cleared)
       if (D == 1) {
         // warp w takes nodes w, w + nwarps, ...; lanes are the node's taps
         for (int q = warp; q < nb; q += nwarps) {
@@ -418,14 +501,15 @@ __global__ void __launch_bounds__(512) k_spread(const typename Cx<T>::t* __restr
           const uint32_t off = (uint32_t)coff[q];
           const int o0 = off & MASK, o1 = (off >> SH) & MASK;
           const int g_first = o0 / R, g_last = (o0 + W - 1) / R;
-          int g0 = g_first + ((warp - g_first % nwarps) + nwarps) % nwarps;
+          const int g0 = g_first + ((warp - g_first % nwarps) + nwarps) % nwarps;
           if (g0 > g_last || !lane_on) continue;
           const T* wq = cw + q * 2 * W;
           const C v = cscale(cval[q], wq[W + l_last]);
+          C* tb = tile + o1 + l_last;
           for (int gg = g0; gg <= g_last; gg += nwarps) {
             const int p0 = gg * R + r;
             if (p0 >= o0 && p0 < o0 + W) {
-              C* p = tile + p0 * S + o1 + l_last;
+              C* p = tb + p0 * S;
               *p = cmul_add(*p, wq[p0 - o0], v);
             }
           }
@@ -434,7 +518,7 @@ __global__ void __launch_bounds__(512) k_spread(const typename Cx<T>::t* __restr
         // warp w owns the planes {p : p % nwarps == w}
         for (int q = 0; q < nb; ++q) {
           const uint32_t off = (uint32_t)coff[q];
-          const int o0 = off & MASK, o1 = (off >> SH) & MASK, o2 = off >> (2 * SH);
+          const int o0 = off & MASK, o1 = (off >> SH) & MASK, o2 = off >> (D == 3 ? 2 * SH : 0);
           int p = o0 + ((warp - o0 % nwarps) + nwarps) % nwarps;
           if (p >= o0 + W || !lane_on) continue;
           const T* wq = cw + q * 3 * W;
@@ -443,17 +527,17 @@ __global__ void __launch_bounds__(512) k_spread(const typename Cx<T>::t* __restr
 #pragma unroll
           for (int it = 0; it < NIT; ++it) {
             const int l1 = r + it * R;
-            vr[it] = cscale(v, l1 < W ? wq[W + l1] : (T)0);
+            vr[it] = cscale(v, (FULL || l1 < W) ? wq[W + (FULL ? l1 : min(l1, W - 1))] : (T)0);
           }
-          const int cbase = (o1 + r) * S + o2 + l_last;
+          C* tb = tile + (o1 + r) * S + o2 + l_last;
           for (; p < o0 + W; p += nwarps) {
-            const T w0 = wq[p - o0];
-            const int pb = p * PS + cbase;
+            const typename WPair<T>::t w0 = WPair<T>::make(wq[p - o0]);
+            C* tp = tb + p * PS;
 #pragma unroll
             for (int it = 0; it < NIT; ++it) {
-              if (r + it * R < W) {
-                C* t = tile + pb + it * R * S;
-                *t = cmul_add(*t, w0, vr[it]);
+              if (FULL || r + it * R < W) {
+                C* t = tp + it * R * S;
+                *t = cmul_addp(*t, w0, vr[it]);
               }
             }
           }
@@ -463,11 +547,10 @@ __global__ void __launch_bounds__(512) k_spread(const typename Cx<T>::t* __restr
     __syncthreads();
     if (D == 1) {
       // fold the private copies into copy 0, then flush
-      const int nw = nwarps;
       for (int e = threadIdx.x; e < tile_elems; e += blockDim.x) {
         C s = tile[e];
-        for (int w = 1; w < nw; ++w) {
-          const C v = reinterpret_cast<C*>(smem + tl.smem_tile + (size_t)(w - 1) * tl.smem_tile)[e];
+        for (int w = 1; w < nwarps; ++w) {
+          const C v = reinterpret_cast<const C*>(smem + (size_t)w * tl.smem_tile)[e];
           s.x += v.x;
           s.y += v.y;
         }
@@ -475,7 +558,7 @@ __global__ void __launch_bounds__(512) k_spread(const typename Cx<T>::t* __restr
       }
       __syncthreads();
     }
-    flush_tile<D, C>(tile, g + o.inst * geo.ntot, geo, tl, o);
+    flush_tile<D, W, C>(tile, g + o.inst * geo.ntot, geo, tl, o);
     __syncthreads();
   }
 }

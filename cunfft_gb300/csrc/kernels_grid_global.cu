@@ -29,7 +29,7 @@ __global__ void __launch_bounds__(128) k_grid_global(const typename Cx<T>::t* __
       T w[kMaxDim][kMaxTaps];
       for (int t = 0; t < D; ++t) {
         s[t] = o.a[t] + ((off >> (off_bits(D) * t)) & ((1u << off_bits(D)) - 1u));
-        WeightMath<T>::taps(sfrac[k * D + t], geo.m, geo.b[t], W, w[t]);
+        WeightMath<T>::taps(sfrac[k * D + t], geo.m, geo, t, W, w[t]);
       }
       const int64_t inst_base = o.inst * geo.ntot;
       if (!SPREAD) {

@@ -70,19 +70,16 @@ static void free_bins(Plan* p) {
   p->bins_capacity_tiles = -1;
 }
 
-// Default tile extents: the padded tile must fit the 227 KB of shared memory a
-// CTA may use; FP32 tiles of the 3D kernels leave room for two CTAs per SM.
+// Default tile extents.  For d >= 2 only the outermost extent T0 is free: the
+// inner extents are the kernels' compile-time values (clamped to the grid).
+// FP32 3D tiles (8 x 8 x 16) leave room for two CTAs per SM.
 static void default_tiles(const Plan* p, int* T) {
-  const int d = p->geo.d;
-  if (d == 1) {
-    T[0] = 2048;
-  } else if (d == 2) {
-    T[0] = 32;
-    T[1] = 64;
-  } else if (p->prec == kF32) {
-    T[0] = 8; T[1] = 4; T[2] = 16;
-  } else {
-    T[0] = 4; T[1] = 4; T[2] = 16;
+  const int d = p->geo.d, W = p->geo.W;
+  T[0] = d == 1 ? 2048 : (d == 2 ? 32 : (p->prec == kF32 ? 8 : 4));
+  if (d == 2) T[1] = fixed_t_last(2, W);
+  if (d == 3) {
+    T[1] = fixed_t_mid(3, W);
+    T[2] = fixed_t_last(3, W);
   }
 }
 
@@ -94,17 +91,23 @@ static Tiling make_tiling(const Plan* p, const int* T, int chunk) {
     tl.nb[t] = t < d ? (int)(p->geo.n[t] / T[t]) : 1;
     tl.E[t] = t < d ? T[t] + W - 1 : 1;
   }
-  const int Elast = tl.E[d - 1];
+  // inner strides are the kernels' compile-time values (inner tiles may be
+  // smaller than the fixed extents when the grid is small)
+  int64_t elems;
   if (d == 1) {
-    tl.S = Elast;
+    tl.S = tl.E[0];
+    tl.R1 = 1;
+    elems = tl.S;
+  } else if (d == 2) {
+    tl.S = fixed_row_stride(2, W);
+    tl.R1 = 1;
+    elems = (int64_t)tl.E[0] * tl.S;
   } else {
-    int S = Elast;
-    while ((S - W) % 16 != 0) ++S;  // S == W (mod 16): conflict-free lane mapping
-    tl.S = S;
+    tl.S = fixed_row_stride(3, W);
+    tl.R1 = fixed_t_mid(3, W) + W - 1;
+    elems = (int64_t)tl.E[0] * tl.R1 * tl.S;
   }
-  tl.R1 = d == 3 ? tl.E[1] : 1;
-  const int64_t rows = d == 3 ? (int64_t)tl.E[0] * tl.E[1] : (d == 2 ? tl.E[0] : 1);
-  tl.smem_tile = (size_t)(rows * tl.S) * elem_bytes(p);
+  tl.smem_tile = (size_t)elems * elem_bytes(p);
   tl.smem_tile = (tl.smem_tile + 15) / 16 * 16;
   tl.tiles_per_inst = (int64_t)tl.nb[0] * tl.nb[1] * tl.nb[2];
   tl.tiles_total = tl.tiles_per_inst * p->geo.batch;
@@ -129,26 +132,23 @@ int plan_choose_tiling(Plan* p, const int* Tin, int chunk) {
   const size_t kMaxSmem = 227 * 1024;
   int T[kMaxDim] = {1, 1, 1};
   default_tiles(p, T);
-  for (int t = 0; t < d; ++t) {
-    if (Tin && Tin[t] > 0) {
-      const int tmax = d == 3 ? 1024 : (d == 2 ? 32768 : (1 << 30));  // packed offset: 30/d bits per dim
-      if (!is_pow2(Tin[t]) || Tin[t] > tmax)
-        return set_status(p, CUNFFT_X_INVALID_ARGUMENT, "tile extent %d is not a power of two <= %d", Tin[t], tmax);
-      T[t] = Tin[t];
-    }
-    if (T[t] > p->geo.n[t]) T[t] = (int)p->geo.n[t];
+  if (Tin && Tin[0] > 0) {
+    const int tmax = d == 3 ? 1024 : (d == 2 ? 32768 : (1 << 30));  // packed offset: 30/d bits per dim
+    if (!is_pow2(Tin[0]) || Tin[0] > tmax)
+      return set_status(p, CUNFFT_X_INVALID_ARGUMENT, "tile extent %d is not a power of two <= %d", Tin[0], tmax);
+    T[0] = Tin[0];
   }
-  int Tfit[kMaxDim] = {T[0], T[1], T[2]};
-  Tiling tl = make_tiling(p, Tfit, chunk);
-  while (smem_of(p, tl) > kMaxSmem) {
-    int big = 0;
-    for (int t = 1; t < d; ++t)
-      if (Tfit[t] > Tfit[big]) big = t;
-    if (Tfit[big] == 1) break;
-    Tfit[big] /= 2;
-    tl = make_tiling(p, Tfit, chunk);
+  for (int t = 0; t < d; ++t)
+    if (T[t] > p->geo.n[t]) T[t] = (int)p->geo.n[t];
+  Tiling tl = make_tiling(p, T, chunk);
+  while (smem_of(p, tl) > kMaxSmem && T[0] > 1) {
+    T[0] /= 2;
+    tl = make_tiling(p, T, chunk);
   }
   if (smem_of(p, tl) > kMaxSmem) {
+    default_tiles(p, T);
+    for (int t = 0; t < d; ++t)
+      if (T[t] > p->geo.n[t]) T[t] = (int)p->geo.n[t];
     tl = make_tiling(p, T, chunk);
     tl.use_global = 1;
     tl.threads = 128;
@@ -193,6 +193,7 @@ int plan_init(Plan* p, int d, const int64_t* N, const int64_t* n, int m, int pre
     g.n[t] = nt;
     const double sigma = (double)nt / (double)N[t];
     g.b[t] = (2.0 * sigma) / (2.0 * sigma - 1.0) * ((double)m / M_PI);
+    g.cbf[t] = (float)(1.4426950408889634 / g.b[t]);
     g.norm *= sqrt((2.0 * sigma - 1.0) / (2.0 * sigma * (double)m));
     g.Ntot *= N[t];
     g.ntot *= nt;
@@ -431,14 +432,11 @@ int plan_autotune(Plan* p, int reps) {
   const int d = p->geo.d;
   std::vector<std::vector<int>> cands;
   if (d == 1) {
-    for (int t : {512, 1024, 2048, 4096, 8192}) cands.push_back({t, 1, 1});
+    for (int t : {512, 1024, 2048, 4096, 8192}) cands.push_back({t, 0, 0});
   } else if (d == 2) {
-    for (int a : {16, 32, 64})
-      for (int b : {32, 64, 128}) cands.push_back({a, b, 1});
-  } else if (p->prec == kF32) {
-    cands = {{8, 4, 16}, {4, 8, 16}, {8, 8, 16}, {16, 16, 16}, {8, 16, 16}, {4, 4, 32}, {8, 4, 32}};
+    for (int a : {8, 16, 32, 64, 128}) cands.push_back({a, 0, 0});
   } else {
-    cands = {{4, 4, 16}, {8, 4, 16}, {4, 8, 16}, {4, 4, 32}, {8, 8, 8}};
+    for (int a : {2, 4, 8, 16}) cands.push_back({a, 0, 0});
   }
   const Tiling best0 = p->tl;
   float best = 3.0e38f;

@@ -283,8 +283,9 @@ def test_tilings_agree(dev, d):
             p = NFFT(N, device=dev).set_nodes(torch.from_numpy(x).to(dev))
             p.set_tiling(T, chunk)
             got_T = p.tiling()["T"]
-            # tiles that do not fit in shared memory are halved until they do
-            assert all(a <= b for a, b in zip(got_T, T)) and p.tiling()["chunk"] == chunk
+            # the outermost extent is tunable (halved until the tile fits in shared
+            # memory); the inner extents are the kernels' compile-time values
+            assert got_T[0] <= T[0] and p.tiling()["chunk"] == chunk
             assert O.rel_l2(ref_f, p.forward(torch.from_numpy(fh).to(dev)).cpu()) < TOL64
             assert O.rel_l2(ref_fh, p.adjoint(torch.from_numpy(f).to(dev)).cpu()) < TOL64
             p.close()
