@@ -84,6 +84,7 @@ X_SYMBOLS = [
     "cunfft_x_interp", "cunfft_x_spread", "cunfft_x_set_stream", "cunfft_x_get_stream", "cunfft_x_set_tiling",
     "cunfft_x_autotune", "cunfft_x_get_tiling", "cunfft_x_stage_times", "cunfft_x_synchronize",
     "cunfft_x_last_message", "cunfft_x_status_string", "cunfft_x_grid", "cunfft_x_version",
+    "cunfft_x_spread_noalloc",
 ]
 UTIL_SYMBOLS = [
     "showTimes", "getGPUMemProps_ToStdout", "showCPUMemUse", "showCoeff_double", "showCoeff_cuComplex",

@@ -159,8 +159,9 @@ int plan_choose_tiling(Plan* p, const int* Tin, int chunk) {
   return CUNFFT_X_SUCCESS;
 }
 
-int plan_init(Plan* p, int d, const int64_t* N, const int64_t* n, int m, int prec, int batch, cudaStream_t stream,
-              void* lend_grid) {
+// Geometry of a plan (parameters, window constants, device attributes); no
+// device or host allocation.
+int geom_init(Plan* p, int d, const int64_t* N, const int64_t* n, int m, int prec, int batch) {
   if (d < 1 || d > kMaxDim) return set_status(p, CUNFFT_X_INVALID_ARGUMENT, "d = %d not in 1..3", d);
   if (m < 1 || 2 * m + 2 > kMaxTaps) return set_status(p, CUNFFT_X_INVALID_ARGUMENT, "m = %d not in 1..15", m);
   if (prec != kF64 && prec != kF32) return set_status(p, CUNFFT_X_INVALID_ARGUMENT, "unknown precision %d", prec);
@@ -203,6 +204,13 @@ int plan_init(Plan* p, int d, const int64_t* N, const int64_t* n, int m, int pre
   CG_TRY(check_cuda(p, cudaGetDevice(&p->device), "cudaGetDevice"));
   CG_TRY(check_cuda(p, cudaDeviceGetAttribute(&p->num_sms, cudaDevAttrMultiProcessorCount, p->device),
                     "cudaDeviceGetAttribute"));
+  return CUNFFT_X_SUCCESS;
+}
+
+int plan_init(Plan* p, int d, const int64_t* N, const int64_t* n, int m, int prec, int batch, cudaStream_t stream,
+              void* lend_grid) {
+  CG_TRY(geom_init(p, d, N, n, m, prec, batch));
+  const Geom& g = p->geo;
   if (stream) {
     p->stream = stream;
     p->own_stream = false;

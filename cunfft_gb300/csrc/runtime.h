@@ -57,6 +57,7 @@ int check_cuda(Plan* p, cudaError_t e, const char* what);
 int check_cufft(Plan* p, cufftResult r, const char* what);
 
 // plan life cycle (plan.cu)
+int geom_init(Plan* p, int d, const int64_t* N, const int64_t* n, int m, int prec, int batch);
 int plan_init(Plan* p, int d, const int64_t* N, const int64_t* n, int m, int prec, int batch,
               cudaStream_t stream, void* lend_grid);
 void plan_release(Plan* p);

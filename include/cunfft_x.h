@@ -89,6 +89,32 @@ int cunfft_x_node_gradient(cunfft_x_plan *plan, const void *f_hat, const void *g
 int cunfft_x_interp(cunfft_x_plan *plan, const void *g, void *f);
 int cunfft_x_spread(cunfft_x_plan *plan, const void *f, void *g);
 
+/** Spreading without any memory allocation (no counterpart in the reference).
+ *
+ *  For callers that cannot allocate device memory: work recorded into a CUDA
+ *  graph by stream capture (cudaMalloc cannot be captured), frameworks whose
+ *  device memory all belongs to their own pool allocator, and real-time loops
+ *  that must not pay for or fail on an allocation.  Same result as
+ *  cunfft_x_spread on a one-instance plan with these parameters: g += spread of
+ *  the samples f at the nodes x, where g is the caller's oversampled grid
+ *  (prod n complex values of the given precision; clear it first for a fresh
+ *  result), x holds M*d doubles and f M complex values, all device pointers,
+ *  asynchronous on `stream` (NULL: the legacy default stream).  n may be NULL
+ *  (n_t = 2*next_pow2(N_t)).
+ *
+ *  Its scratch (node bins, tile counts, work queue) is one fixed device array
+ *  inside the library, about 42 MB, which every GPU that loads the library holds
+ *  until the process exits.  Limits: M <= 1048576 nodes and at most 65536 grid
+ *  tiles (every 3D grid up to 256^3 and every 2D grid up to 8192^2 fits); larger
+ *  requests return
+ *  CUNFFT_X_INVALID_ARGUMENT with a message on stderr.  The first call on each
+ *  device looks up the array's device address; make that first call outside
+ *  any stream capture.  All calls share the array: calls that overlap on the
+ *  GPU (other streams, other host threads on the same device) race and must be
+ *  serialised by the caller. */
+int cunfft_x_spread_noalloc(int d, const int64_t *N, const int64_t *n, int m, int precision, int64_t M,
+                            const double *x, const void *f, void *g, void *stream);
+
 /** Stream used by the plan (cudaStream_t as void*). */
 int cunfft_x_set_stream(cunfft_x_plan *plan, void *stream);
 void *cunfft_x_get_stream(const cunfft_x_plan *plan);
