@@ -79,7 +79,7 @@ ABI_SYMBOLS = [
 ]
 X_SYMBOLS = [
     "cunfft_x_plan_create", "cunfft_x_plan_destroy", "cunfft_x_set_nodes", "cunfft_x_forward",
-    "cunfft_x_adjoint", "cunfft_x_ndft_forward", "cunfft_x_ndft_adjoint", "cunfft_x_ndft_adjoint_at",
+    "cunfft_x_adjoint", "cunfft_x_forward_graph", "cunfft_x_adjoint_graph", "cunfft_x_ndft_forward", "cunfft_x_ndft_adjoint", "cunfft_x_ndft_adjoint_at",
     "cunfft_x_node_gradient",
     "cunfft_x_interp", "cunfft_x_spread", "cunfft_x_set_stream", "cunfft_x_get_stream", "cunfft_x_set_tiling",
     "cunfft_x_autotune", "cunfft_x_get_tiling", "cunfft_x_stage_times", "cunfft_x_synchronize",
@@ -114,6 +114,10 @@ def lib():
         "cunfft_x_set_nodes": (ctypes.c_int, [vp, vp, i64p]),
         "cunfft_x_forward": (ctypes.c_int, [vp, vp, vp]),
         "cunfft_x_adjoint": (ctypes.c_int, [vp, vp, vp]),
+        "cunfft_x_forward_graph": (ctypes.c_int, [vp, vp, vp]),
+        "cunfft_x_adjoint_graph": (ctypes.c_int, [vp, vp, vp]),
+        "cunfft_x_spread_noalloc": (ctypes.c_int, [ctypes.c_int, i64p, i64p, ctypes.c_int, ctypes.c_int,
+                                                   ctypes.c_int64, vp, vp, vp, vp]),
         "cunfft_x_ndft_forward": (ctypes.c_int, [vp, vp, vp]),
         "cunfft_x_ndft_adjoint": (ctypes.c_int, [vp, vp, vp]),
         "cunfft_x_ndft_adjoint_at": (ctypes.c_int, [vp, vp, vp, ctypes.c_int64, vp]),

@@ -48,9 +48,12 @@ __global__ void __launch_bounds__(256) k_ndft_forward(const double* __restrict__
     sincospi(-2.0 * xj[d - 1], &sr, &cr);
     const double2 rot = make_double2(cr, sr);
     double2 acc = make_double2(0.0, 0.0), ph = make_double2(1.0, 0.0);
-    int64_t pos = 0;  // position inside the current row of the last dimension
-    for (int64_t c0 = 0; c0 < geo.Ntot; c0 += kNdftChunk) {
-      const int cn = (int)min((int64_t)kNdftChunk, geo.Ntot - c0);
+    // split of the coefficient range over blockIdx.z (partial sums added atomically)
+    const int64_t span = ((geo.Ntot + gridDim.z - 1) / gridDim.z + kNdftChunk - 1) / kNdftChunk * kNdftChunk;
+    const int64_t c_lo = (int64_t)blockIdx.z * span, c_hi = min(geo.Ntot, c_lo + span);
+    int64_t pos = c_lo % Nlast;  // position inside the current row of the last dimension
+    for (int64_t c0 = c_lo; c0 < c_hi; c0 += kNdftChunk) {
+      const int cn = (int)min((int64_t)kNdftChunk, c_hi - c0);
       __syncthreads();
       if (threadIdx.x < cn) sfh[threadIdx.x] = fh[c0 + threadIdx.x];
       __syncthreads();
@@ -73,7 +76,14 @@ __global__ void __launch_bounds__(256) k_ndft_forward(const double* __restrict__
         if (++pos == Nlast) pos = 0;
       }
     }
-    if (on) f[j] = acc;
+    if (on) {
+      if (gridDim.z == 1) {
+        f[j] = acc;
+      } else {
+        atomicAdd(&f[j].x, acc.x);
+        atomicAdd(&f[j].y, acc.y);
+      }
+    }
   }
 }
 
@@ -102,8 +112,11 @@ __global__ void __launch_bounds__(256) k_ndft_adjoint(const double* __restrict__
       }
     }
     double2 acc = make_double2(0.0, 0.0);
-    for (int64_t c0 = j0; c0 < j1; c0 += kNdftChunk) {
-      const int cn = (int)min((int64_t)kNdftChunk, j1 - c0);
+    // split of the node range over blockIdx.z (partial sums added atomically)
+    const int64_t span = ((j1 - j0 + gridDim.z - 1) / gridDim.z + kNdftChunk - 1) / kNdftChunk * kNdftChunk;
+    const int64_t n_lo = j0 + (int64_t)blockIdx.z * span, n_hi = min(j1, n_lo + span);
+    for (int64_t c0 = n_lo; c0 < n_hi; c0 += kNdftChunk) {
+      const int cn = (int)min((int64_t)kNdftChunk, n_hi - c0);
       __syncthreads();
       for (int e = threadIdx.x; e < cn * d; e += blockDim.x) sx[e] = x[c0 * d + e];
       if (threadIdx.x < cn) sf[threadIdx.x] = f[c0 + threadIdx.x];
@@ -116,8 +129,27 @@ __global__ void __launch_bounds__(256) k_ndft_adjoint(const double* __restrict__
         acc = cfma(sf[s], make_double2(cp, sp), acc);
       }
     }
-    if (on) out[kl] = acc;
+    if (on) {
+      if (gridDim.z == 1) {
+        out[kl] = acc;
+      } else {
+        atomicAdd(&out[kl].x, acc.x);
+        atomicAdd(&out[kl].y, acc.y);
+      }
+    }
   }
+}
+
+// Few outputs (e.g. a 4096-node check of a large transform) would occupy a few
+// SMs only: split the inner sum over up to 4 CTAs per SM, at least 4096 terms each.
+static int ndft_splits(const Plan& p, int64_t blocks, int64_t inner) {
+  const int64_t want = (int64_t)p.num_sms * 4;
+  if (blocks >= want) return 1;
+  int64_t s = (want + blocks - 1) / blocks;
+  const int64_t cap = (inner + 4095) / 4096;
+  if (s > cap) s = cap;
+  if (s > 65535) s = 65535;
+  return (int)(s < 1 ? 1 : s);
 }
 
 cudaError_t launch_ndft_forward(const Plan& p, const double* x, const void* fhat, void* f, cudaStream_t st) {
@@ -126,7 +158,12 @@ cudaError_t launch_ndft_forward(const Plan& p, const double* x, const void* fhat
   if (maxM == 0) return cudaSuccess;
   int64_t bx = (maxM + 255) / 256;
   if (bx > (int64_t)p.num_sms * 8) bx = (int64_t)p.num_sms * 8;
-  dim3 grid((unsigned)bx, (unsigned)p.geo.batch);
+  const int splits = ndft_splits(p, bx * p.geo.batch, p.geo.Ntot);
+  if (splits > 1) {
+    const cudaError_t e = cudaMemsetAsync(f, 0, sizeof(double2) * p.M, st);
+    if (e != cudaSuccess) return e;
+  }
+  dim3 grid((unsigned)bx, (unsigned)p.geo.batch, (unsigned)splits);
   k_ndft_forward<<<grid, 256, 0, st>>>(x, (const double2*)fhat, (double2*)f, p.geo, p.bins.inst_off);
   return cudaGetLastError();
 }
@@ -137,7 +174,14 @@ cudaError_t launch_ndft_adjoint(const Plan& p, const double* x, const void* f, v
   if (nout == 0) return cudaSuccess;
   int64_t bx = (nout + 255) / 256;
   if (bx > (int64_t)p.num_sms * 8) bx = (int64_t)p.num_sms * 8;
-  dim3 grid((unsigned)bx, (unsigned)p.geo.batch);
+  int64_t maxM = 0;
+  for (int i = 0; i < p.geo.batch; ++i) maxM = p.M_inst[i] > maxM ? p.M_inst[i] : maxM;
+  const int splits = ndft_splits(p, bx * p.geo.batch, maxM);
+  if (splits > 1) {
+    const cudaError_t e = cudaMemsetAsync(fhat, 0, sizeof(double2) * nout * p.geo.batch, st);
+    if (e != cudaSuccess) return e;
+  }
+  dim3 grid((unsigned)bx, (unsigned)p.geo.batch, (unsigned)splits);
   k_ndft_adjoint<<<grid, 256, 0, st>>>(x, (const double2*)f, (double2*)fhat, p.geo, p.bins.inst_off, kidx, nsel);
   return cudaGetLastError();
 }

@@ -276,6 +276,11 @@ int plan_init(Plan* p, int d, const int64_t* N, const int64_t* n, int m, int pre
 void plan_release(Plan* p) {
   if (!p) return;
   if (p->stream) cudaStreamSynchronize(p->stream);
+  for (int i = 0; i < 2; ++i)
+    if (p->gexec[i]) {
+      cudaGraphExecDestroy(p->gexec[i]);
+      p->gexec[i] = nullptr;
+    }
   free_bins(p);
   cudaFree(p->bins.inst_off);
   cudaFree(p->bins.work);
@@ -331,6 +336,7 @@ static int rebin(Plan* p) {
   CG_TRY(check_cuda(p, launch_binning(*p, p->x, p->stream), "binning kernels"));
   if (p->timing) cudaEventRecord(p->ev[7], p->stream);
   p->bins.valid = 1;
+  ++p->node_gen;  // captured graphs hold the old binning by value
   return CUNFFT_X_SUCCESS;
 }
 
@@ -393,6 +399,45 @@ int plan_adjoint(Plan* p, const void* f, void* fhat) {
   rec(p, 2);
   CG_TRY(check_cuda(p, launch_roc_adjoint(*p, p->g, fhat, p->stream), "roll-off kernel"));
   rec(p, 3);
+  return set_status(p, CUNFFT_X_SUCCESS, nullptr);
+}
+
+// Forward (adjoint = 0) or adjoint (1) through a CUDA graph.  The stage
+// sequence (roll-off, FFT, gridding and the small memsets) is captured from the
+// plan's stream once per (input, output, node binding) and then replayed with one
+// cudaGraphLaunch; the node binning itself stays outside the graph.
+int plan_run_graph(Plan* p, int adjoint, const void* in, void* out) {
+  if (!p->nodes_set) return set_status(p, CUNFFT_X_NODES_NOT_SET, "graph: nodes not set");
+  if (!p->bins.valid) CG_TRY(rebin(p));
+  const int k = adjoint ? 1 : 0;
+  if (!p->gexec[k] || p->g_in[k] != in || p->g_out[k] != out || p->g_gen[k] != p->node_gen) {
+    if (p->gexec[k]) {
+      cudaGraphExecDestroy(p->gexec[k]);
+      p->gexec[k] = nullptr;
+    }
+    // run once uncaptured so that every kernel attribute and cuFFT resource is set up
+    CG_TRY(adjoint ? plan_adjoint(p, in, out) : plan_forward(p, in, out));
+    const bool timing = p->timing;
+    p->timing = false;
+    cudaGraph_t graph = nullptr;
+    CG_TRY(check_cuda(p, cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal), "begin capture"));
+    const int s = adjoint ? plan_adjoint(p, in, out) : plan_forward(p, in, out);
+    const cudaError_t ec = cudaStreamEndCapture(p->stream, &graph);
+    p->timing = timing;
+    if (s != CUNFFT_X_SUCCESS) {
+      if (graph) cudaGraphDestroy(graph);
+      return s;
+    }
+    CG_TRY(check_cuda(p, ec, "end capture"));
+    const cudaError_t ei = cudaGraphInstantiate(&p->gexec[k], graph, 0);
+    cudaGraphDestroy(graph);
+    CG_TRY(check_cuda(p, ei, "instantiate graph"));
+    p->g_in[k] = in;
+    p->g_out[k] = out;
+    p->g_gen[k] = p->node_gen;
+    return set_status(p, CUNFFT_X_SUCCESS, nullptr);  // this call's result came from the uncaptured run
+  }
+  CG_TRY(check_cuda(p, cudaGraphLaunch(p->gexec[k], p->stream), "graph launch"));
   return set_status(p, CUNFFT_X_SUCCESS, nullptr);
 }
 

@@ -49,6 +49,12 @@ struct Plan {
   cudaEvent_t ev[8] = {};
   bool timing = false;
   double t_bin = 0, t_roc = 0, t_fft = 0, t_conv = 0;
+  // CUDA graphs of the forward [0] and adjoint [1] stage sequences
+  cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+  const void* g_in[2] = {nullptr, nullptr};
+  void* g_out[2] = {nullptr, nullptr};
+  uint64_t g_gen[2] = {0, 0};
+  uint64_t node_gen = 0;  // bumped by every node binding / tiling change
 };
 
 // status helpers
@@ -64,6 +70,7 @@ void plan_release(Plan* p);
 int plan_set_nodes(Plan* p, const double* x, const int64_t* M_inst);
 int plan_forward(Plan* p, const void* fhat, void* f);
 int plan_adjoint(Plan* p, const void* f, void* fhat);
+int plan_run_graph(Plan* p, int adjoint, const void* in, void* out);
 int plan_interp_only(Plan* p, const void* g, void* f);
 int plan_spread_only(Plan* p, const void* f, void* g);
 int plan_ndft_forward(Plan* p, const void* fhat, void* f);

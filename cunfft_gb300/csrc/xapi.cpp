@@ -49,6 +49,16 @@ int cunfft_x_adjoint(cunfft_x_plan* h, const void* f, void* fhat) {
   return cg::plan_adjoint(&h->p, f, fhat);
 }
 
+int cunfft_x_forward_graph(cunfft_x_plan* h, const void* fhat, void* f) {
+  if (!h || (!fhat && h->p.geo.Ntot) || (!f && h->p.M)) return CUNFFT_X_INVALID_ARGUMENT;
+  return cg::plan_run_graph(&h->p, 0, fhat, f);
+}
+
+int cunfft_x_adjoint_graph(cunfft_x_plan* h, const void* f, void* fhat) {
+  if (!h || (!fhat && h->p.geo.Ntot) || (!f && h->p.M)) return CUNFFT_X_INVALID_ARGUMENT;
+  return cg::plan_run_graph(&h->p, 1, f, fhat);
+}
+
 int cunfft_x_ndft_forward(cunfft_x_plan* h, const void* fhat, void* f) {
   if (!h) return CUNFFT_X_INVALID_ARGUMENT;
   return cg::plan_ndft_forward(&h->p, fhat, f);

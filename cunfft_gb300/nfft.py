@@ -112,6 +112,18 @@ class NFFT:
         nat.check(self._lib.cunfft_x_adjoint(self._h, _ptr(f), _ptr(fh)), self._h)
         return fh
 
+    def forward_graph(self, fhat, out):
+        """forward() replayed from a captured CUDA graph (fixed buffers fhat, out)."""
+        fhat = self._coef(fhat)
+        nat.check(self._lib.cunfft_x_forward_graph(self._h, _ptr(fhat), _ptr(out)), self._h)
+        return out
+
+    def adjoint_graph(self, f, out):
+        """adjoint() replayed from a captured CUDA graph (fixed buffers f, out)."""
+        f = self._samples(f)
+        nat.check(self._lib.cunfft_x_adjoint_graph(self._h, _ptr(f), _ptr(out)), self._h)
+        return out
+
     def ndft_forward(self, fhat):
         fhat = fhat.to(torch.complex128).contiguous()
         f = torch.empty(self.M, dtype=torch.complex128, device=self.device)

@@ -66,6 +66,16 @@ int cunfft_x_forward(cunfft_x_plan *plan, const void *f_hat, void *f);
 /** f_hat = A^H f for every instance. */
 int cunfft_x_adjoint(cunfft_x_plan *plan, const void *f, void *f_hat);
 
+/** cunfft_x_forward / cunfft_x_adjoint through a CUDA graph.  The first call
+ *  for a given (input, output) pair and node binding runs the transform and
+ *  captures its stage sequence (roll-off, FFT, gridding of all instances) from
+ *  the plan's stream into an instantiated graph; later calls replay it with a
+ *  single cudaGraphLaunch.  Binding new nodes or changing the tiling triggers a
+ *  new capture.  The plan's stream must be capturable (not the legacy NULL
+ *  stream nor a stream that synchronises with it). */
+int cunfft_x_forward_graph(cunfft_x_plan *plan, const void *f_hat, void *f);
+int cunfft_x_adjoint_graph(cunfft_x_plan *plan, const void *f, void *f_hat);
+
 /** Direct NDFT and adjoint NDFT on the bound nodes, always in FP64 with
  *  complex128 buffers, whatever the plan precision (the error yardstick). */
 int cunfft_x_ndft_forward(cunfft_x_plan *plan, const void *f_hat, void *f);

@@ -90,7 +90,9 @@ def test_abi_reproduces_reference_kat(dev, k):
     assert O.rel_l2(ref_nfft, got) < TOL64
     assert O.rel_l2(ref_ndft, nd) < TOL_NDFT
     e = O.error_l_infty(nd, got)
-    tol = 1e-3 if m <= 8 else 1e-2
+    # m = 12 values (~5e-13) sit at the rounding level of the NDFT sums, whose
+    # order (split over thread blocks) moves them by about 1%
+    tol = 1e-3 if m <= 8 else 3e-2
     assert abs(e / k["e_inf"] - 1) < tol, (e, k["e_inf"])
     assert times["time_FFT"] > 0 and times["time_CONV"] > 0
 
