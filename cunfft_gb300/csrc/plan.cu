@@ -155,8 +155,28 @@ int plan_choose_tiling(Plan* p, const int* Tin, int chunk) {
   }
   if (tl.tiles_total >= (int64_t)1 << 31) return set_status(p, CUNFFT_X_INVALID_ARGUMENT, "too many tiles");
   p->tl = tl;
+  p->tl.spread_reg = p->spread_mode != CUNFFT_X_SPREAD_SHARED && spread_reg_supported(*p);
   p->bins.valid = 0;
   return CUNFFT_X_SUCCESS;
+}
+
+int plan_spread_kernel(const Plan* p) {
+  if (p->tl.use_global) return CUNFFT_X_SPREAD_GLOBAL;
+  return p->tl.spread_reg ? CUNFFT_X_SPREAD_REGISTER : CUNFFT_X_SPREAD_SHARED;
+}
+
+// The kernel choice changes only the spreading launch, not the bins; captured
+// graphs are invalidated through node_gen.
+int plan_set_spread_kernel(Plan* p, int kind) {
+  if (kind != CUNFFT_X_SPREAD_AUTO && kind != CUNFFT_X_SPREAD_SHARED && kind != CUNFFT_X_SPREAD_REGISTER)
+    return set_status(p, CUNFFT_X_INVALID_ARGUMENT, "unknown spreading kernel %d", kind);
+  if (kind == CUNFFT_X_SPREAD_REGISTER && !spread_reg_supported(*p))
+    return set_status(p, CUNFFT_X_UNSUPPORTED,
+                      "register spreading needs d = 3, FP32, 2m+2 <= 16 and an outer tile extent <= 8");
+  p->spread_mode = kind;
+  p->tl.spread_reg = kind != CUNFFT_X_SPREAD_SHARED && spread_reg_supported(*p);
+  ++p->node_gen;
+  return set_status(p, CUNFFT_X_SUCCESS, nullptr);
 }
 
 // Geometry of a plan (parameters, window constants, device attributes); no
@@ -477,8 +497,9 @@ int plan_node_gradient(Plan* p, const void* fhat, const void* grad_f, double* gr
 }
 
 // Autotuner: time interpolation and spreading for a few tilings on the bound
-// node set; keep the tiling with the smallest sum.  Restores the previous tiling
-// when a candidate fails.
+// node set (and, where the register-tile spreading kernel applies and no kernel
+// was requested, both spreading kernels); keep the fastest sum.  Restores the
+// previous tiling when a candidate fails.
 int plan_autotune(Plan* p, int reps) {
   if (!p->nodes_set) return set_status(p, CUNFFT_X_NODES_NOT_SET, "autotune: nodes not set");
   if (reps < 1) reps = 1;
@@ -494,6 +515,7 @@ int plan_autotune(Plan* p, int reps) {
   const Tiling best0 = p->tl;
   float best = 3.0e38f;
   std::vector<int> best_T(3, 0);
+  int best_reg = 0;
   const size_t bytes = elem_bytes(p);
   void* scratch_f = nullptr;
   if (check_cuda(p, cudaMalloc(&scratch_f, bytes * std::max<int64_t>(p->M, 1)), "autotune scratch")) return p->last_status;
@@ -512,22 +534,34 @@ int plan_autotune(Plan* p, int reps) {
     if (!fits) continue;
     if (plan_choose_tiling(p, T, p->chunk_override) != CUNFFT_X_SUCCESS) continue;
     if (rebin(p) != CUNFFT_X_SUCCESS) break;
-    // warm-up
-    if (launch_interp(*p, p->g, scratch_f, p->stream) != cudaSuccess) continue;
-    if (launch_spread(*p, scratch_f, p->g, p->stream) != cudaSuccess) continue;
-    cudaEventRecord(a, p->stream);
-    for (int r = 0; r < reps; ++r) {
-      launch_interp(*p, p->g, scratch_f, p->stream);
-      launch_spread(*p, scratch_f, p->g, p->stream);
+    // both spreading kernels where the choice is open
+    std::vector<int> kinds{p->tl.spread_reg};
+    if (p->spread_mode == CUNFFT_X_SPREAD_AUTO && p->tl.spread_reg) kinds.push_back(0);
+    bool failed = false;
+    for (int kind : kinds) {
+      p->tl.spread_reg = kind;
+      // warm-up
+      if (launch_interp(*p, p->g, scratch_f, p->stream) != cudaSuccess) continue;
+      if (launch_spread(*p, scratch_f, p->g, p->stream) != cudaSuccess) continue;
+      cudaEventRecord(a, p->stream);
+      for (int r = 0; r < reps; ++r) {
+        launch_interp(*p, p->g, scratch_f, p->stream);
+        launch_spread(*p, scratch_f, p->g, p->stream);
+      }
+      cudaEventRecord(b, p->stream);
+      if (cudaEventSynchronize(b) != cudaSuccess) {
+        failed = true;
+        break;
+      }
+      float ms = 0;
+      cudaEventElapsedTime(&ms, a, b);
+      if (ms < best) {
+        best = ms;
+        best_T = {T[0], T[1], T[2]};
+        best_reg = kind;
+      }
     }
-    cudaEventRecord(b, p->stream);
-    if (cudaEventSynchronize(b) != cudaSuccess) break;
-    float ms = 0;
-    cudaEventElapsedTime(&ms, a, b);
-    if (ms < best) {
-      best = ms;
-      best_T = {T[0], T[1], T[2]};
-    }
+    if (failed) break;
   }
   p->timing = timing;
   cudaEventDestroy(a);
@@ -541,6 +575,7 @@ int plan_autotune(Plan* p, int reps) {
   }
   int T[3] = {best_T[0], best_T[1], best_T[2]};
   CG_TRY(plan_choose_tiling(p, T, p->chunk_override));
+  p->tl.spread_reg = best_reg;
   CG_TRY(rebin(p));
   // the grid holds garbage from the timing runs; transforms rewrite it fully
   p->autotuned = true;

@@ -42,6 +42,7 @@ struct Plan {
   bool nodes_set = false;
   int tile_override[kMaxDim] = {0, 0, 0};
   int chunk_override = 0;
+  int spread_mode = CUNFFT_X_SPREAD_AUTO;  // requested spreading kernel
   bool autotuned = false;
   int last_status = 0;
   char last_msg[256] = {0};
@@ -78,6 +79,13 @@ int plan_ndft_adjoint(Plan* p, const void* f, void* fhat, const int64_t* kidx = 
 int plan_node_gradient(Plan* p, const void* fhat, const void* grad_f, double* grad_x);
 int plan_choose_tiling(Plan* p, const int* T, int chunk);
 int plan_autotune(Plan* p, int reps);
+int plan_set_spread_kernel(Plan* p, int kind);
+int plan_spread_kernel(const Plan* p);
+
+// register-tile spreading kernel (grid_spread_reg.cu)
+bool spread_reg_supported(const Plan& p);
+size_t spread_reg_smem_bytes(const Plan& p);
+cudaError_t grid_launch_spread_reg(const Plan& p, const void* f, void* g, cudaStream_t st);
 
 // launchers (kernel .cu files); all asynchronous on st
 cudaError_t launch_binning(const Plan& p, const double* x, cudaStream_t st);

@@ -174,7 +174,19 @@ class NFFT:
         T = (ctypes.c_int * 3)()
         chunk, threads = ctypes.c_int(), ctypes.c_int()
         nat.check(self._lib.cunfft_x_get_tiling(self._h, T, ctypes.byref(chunk), ctypes.byref(threads)))
-        return {"T": list(T)[: self.d], "chunk": chunk.value, "threads": threads.value}
+        return {"T": list(T)[: self.d], "chunk": chunk.value, "threads": threads.value, "spread": self.spread_kernel()}
+
+    SPREAD_KERNELS = {"auto": 0, "shared": 1, "register": 2, "global": 3}
+
+    def set_spread_kernel(self, kind="auto"):
+        """Request the spreading kernel: "auto", "shared" or "register"."""
+        nat.check(self._lib.cunfft_x_set_spread_kernel(self._h, self.SPREAD_KERNELS[kind]), self._h)
+
+    def spread_kernel(self):
+        """Spreading kernel in use: "shared", "register" or "global"."""
+        k = ctypes.c_int()
+        nat.check(self._lib.cunfft_x_get_spread_kernel(self._h, ctypes.byref(k)))
+        return {v: n for n, v in self.SPREAD_KERNELS.items()}[k.value]
 
     def autotune(self, reps=3):
         nat.check(self._lib.cunfft_x_autotune(self._h, int(reps)), self._h)

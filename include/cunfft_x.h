@@ -28,6 +28,16 @@ extern "C" {
  *  FP32 keeps FP64 only for the node-to-grid reduction and the roll-off factors. */
 enum { CUNFFT_X_F64 = 0, CUNFFT_X_F32 = 1 };
 
+/** Spreading (adjoint gridding) kernel.  AUTO picks REGISTER where it applies
+ *  (d = 3, FP32, 2m+2 <= 16, outer tile extent <= 8) and SHARED elsewhere;
+ *  GLOBAL is reported when no shared-memory tile fits (wide 3D windows). */
+enum {
+  CUNFFT_X_SPREAD_AUTO = 0,
+  CUNFFT_X_SPREAD_SHARED = 1,   /* padded tile in shared memory, warp-owned planes */
+  CUNFFT_X_SPREAD_REGISTER = 2, /* padded tile in registers, one warp per plane */
+  CUNFFT_X_SPREAD_GLOBAL = 3    /* atomics straight into the grid (fallback) */
+};
+
 /** Status codes returned by every cunfft_x_* entry point. */
 enum cunfft_x_status {
   CUNFFT_X_SUCCESS = 0,
@@ -140,6 +150,14 @@ int cunfft_x_autotune(cunfft_x_plan *plan, int reps);
 
 /** Current tiling: T[3], chunk, threads (any pointer may be NULL). */
 int cunfft_x_get_tiling(const cunfft_x_plan *plan, int *T, int *chunk, int *threads);
+
+/** Request a spreading kernel (CUNFFT_X_SPREAD_AUTO, _SHARED or _REGISTER).
+ *  REGISTER on a plan it does not cover returns CUNFFT_X_UNSUPPORTED and keeps
+ *  the current kernel.  The request holds across later tilings. */
+int cunfft_x_set_spread_kernel(cunfft_x_plan *plan, int kind);
+
+/** Spreading kernel in use: CUNFFT_X_SPREAD_SHARED, _REGISTER or _GLOBAL. */
+int cunfft_x_get_spread_kernel(const cunfft_x_plan *plan, int *kind);
 
 /** Per-stage device times of the last forward/adjoint call, in seconds
  *  (binning, roll-off, FFT, gridding).  Blocks until the plan stream is idle. */

@@ -1,0 +1,184 @@
+"""Register-tile spreading kernel (3D FP32, 2m+2 <= 16) against the shared-tile
+kernel and the oracle; kernel selection through the extension API."""
+import numpy as np
+import pytest
+
+import oracle as O
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+TOL32 = 1e-5     # FP32 form vs the FP64 oracle (relative l2), as the parity tests
+TOL_KERN = 2e-6  # the two FP32 spreading kernels against each other: summation order only
+
+
+@pytest.fixture(scope="module")
+def dev():
+    from cunfft_gb300 import _native
+    _native.lib()
+    return torch.device("cuda:0")
+
+
+def _rand(shape, rng):
+    return rng.uniform(-1, 1, shape) + 1j * rng.uniform(-1, 1, shape)
+
+
+def _spread_both(p, f):
+    assert p.spread_kernel() == "register"
+    g_reg = p.spread(f).clone()
+    p.set_spread_kernel("shared")
+    assert p.spread_kernel() == "shared"
+    g_sh = p.spread(f).clone()
+    p.set_spread_kernel("auto")
+    return g_reg, g_sh
+
+
+@pytest.mark.parametrize("m", [1, 2, 3, 4, 5, 6, 7])
+def test_register_matches_shared_every_width(dev, m):
+    from cunfft_gb300.nfft import NFFT
+    rng = np.random.default_rng(100 + m)
+    N, M = [32, 32, 32], 30000
+    x = rng.uniform(-0.5, 0.5, (M, 3))
+    f = _rand(M, rng)
+    p = NFFT(N, m=m, precision="f32", device=dev).set_nodes(torch.from_numpy(x).to(dev))
+    ft = torch.from_numpy(f).to(dev)
+    g_reg, g_sh = _spread_both(p, ft)
+    assert O.rel_l2(g_sh.cpu().numpy(), g_reg.cpu().numpy()) < TOL_KERN
+    assert O.rel_l2(O.nfft_adjoint(x, f, N, m=m), p.adjoint(ft).cpu()) < TOL32
+    p.close()
+
+
+@pytest.mark.parametrize("T0", [1, 2, 4, 8])
+def test_register_outer_tile_extents(dev, T0):
+    from cunfft_gb300.nfft import NFFT
+    rng = np.random.default_rng(7 + T0)
+    N, M = [16, 32, 64], 20000
+    x = rng.uniform(-0.5, 0.5, (M, 3))
+    f = _rand(M, rng)
+    p = NFFT(N, m=6, precision="f32", device=dev).set_nodes(torch.from_numpy(x).to(dev))
+    p.set_tiling([T0])
+    assert p.tiling()["T"][0] == T0
+    g_reg, g_sh = _spread_both(p, torch.from_numpy(f).to(dev))
+    assert O.rel_l2(g_sh.cpu().numpy(), g_reg.cpu().numpy()) < TOL_KERN
+    p.close()
+
+
+@pytest.mark.parametrize("N", [[4, 4, 4], [8, 2, 16], [2, 8, 4], [64, 8, 4]])
+def test_register_small_and_ragged_grids(dev, N):
+    """Grids smaller than the fixed inner tile (8 x 16): the padded tile wraps onto
+    itself and lane pairs straddle nothing."""
+    from cunfft_gb300.nfft import NFFT
+    rng = np.random.default_rng(sum(N))
+    M = 3000
+    x = rng.uniform(-0.5, 0.5, (M, 3))
+    f = _rand(M, rng)
+    p = NFFT(N, m=3, precision="f32", device=dev).set_nodes(torch.from_numpy(x).to(dev))
+    ft = torch.from_numpy(f).to(dev)
+    g_reg, g_sh = _spread_both(p, ft)
+    assert O.rel_l2(g_sh.cpu().numpy(), g_reg.cpu().numpy()) < TOL_KERN
+    assert O.rel_l2(O.nfft_adjoint(x, f, N, m=3), p.adjoint(ft).cpu()) < 5 * TOL32
+    p.close()
+
+
+def test_register_clustered_and_boundary_nodes(dev):
+    """Many nodes in a few tiles (long work-item chains), nodes on -1/2 and near +1/2."""
+    from cunfft_gb300.nfft import NFFT
+    rng = np.random.default_rng(5)
+    N, M = [32, 32, 32], 40000
+    x = np.clip(rng.normal(0.1, 0.02, (M, 3)), -0.5, 0.4999)
+    x[:50] = -0.5
+    x[50:100] = np.nextafter(0.5, 0)
+    x[100:150] = -0.0
+    f = _rand(M, rng)
+    p = NFFT(N, m=6, precision="f32", device=dev).set_nodes(torch.from_numpy(x).to(dev))
+    ft = torch.from_numpy(f).to(dev)
+    g_reg, g_sh = _spread_both(p, ft)
+    assert O.rel_l2(g_sh.cpu().numpy(), g_reg.cpu().numpy()) < TOL_KERN
+    assert O.rel_l2(O.nfft_adjoint(x, f, N), p.adjoint(ft).cpu()) < TOL32
+    p.close()
+
+
+def test_register_batched_uneven(dev):
+    from cunfft_gb300.nfft import NFFT
+    rng = np.random.default_rng(11)
+    N, Ms = [16, 16, 16], [5000, 0, 1234]
+    xs = [rng.uniform(-0.5, 0.5, (M, 3)) for M in Ms]
+    fs = [_rand(M, rng) for M in Ms]
+    p = NFFT(N, m=5, precision="f32", batch=3, device=dev)
+    p.set_nodes(torch.from_numpy(np.concatenate(xs)).to(dev), M_inst=Ms)
+    ft = torch.from_numpy(np.concatenate(fs)).to(dev)
+    g_reg, g_sh = _spread_both(p, ft)
+    assert O.rel_l2(g_sh.cpu().numpy(), g_reg.cpu().numpy()) < TOL_KERN
+    got = p.adjoint(ft).cpu().numpy()
+    for i in range(3):
+        if Ms[i]:
+            assert O.rel_l2(O.nfft_adjoint(xs[i], fs[i], N, m=5), got[i]) < TOL32
+        else:
+            assert np.abs(got[i]).max() == 0
+    p.close()
+
+
+def test_register_graph_follows_kernel_choice(dev):
+    from cunfft_gb300.nfft import NFFT
+    rng = np.random.default_rng(12)
+    N, M = [32, 32, 32], 20000
+    x = rng.uniform(-0.5, 0.5, (M, 3))
+    f = torch.from_numpy(_rand(M, rng)).to(dev).to(torch.complex64)
+    p = NFFT(N, precision="f32", device=dev).set_nodes(torch.from_numpy(x).to(dev))
+    out = torch.empty(N, dtype=torch.complex64, device=dev)
+    p.adjoint_graph(f, out)
+    a = out.clone()
+    p.set_spread_kernel("shared")
+    p.adjoint_graph(f, out)
+    b = out.clone()
+    torch.cuda.synchronize()
+    assert O.rel_l2(a.cpu().numpy(), b.cpu().numpy()) < TOL_KERN
+    assert O.rel_l2(p.adjoint(f).cpu().numpy(), b.cpu().numpy()) < TOL_KERN
+    p.close()
+
+
+def test_kernel_selection_rules(dev):
+    from cunfft_gb300._native import CunfftError
+    from cunfft_gb300.nfft import NFFT
+    x3 = torch.rand(100, 3, dtype=torch.float64, device=dev) - 0.5
+    # FP64 and 2D plans: the register kernel does not apply
+    p = NFFT([16, 16, 16], precision="f64", device=dev).set_nodes(x3)
+    assert p.spread_kernel() == "shared"
+    with pytest.raises(CunfftError):
+        p.set_spread_kernel("register")
+    p.close()
+    p = NFFT([32, 32], precision="f32", device=dev).set_nodes(x3[:, :2].contiguous())
+    assert p.spread_kernel() == "shared"
+    with pytest.raises(CunfftError):
+        p.set_spread_kernel("register")
+    p.close()
+    # W = 18 > 16
+    p = NFFT([16, 16, 16], m=8, precision="f32", device=dev).set_nodes(x3)
+    assert p.spread_kernel() == "shared"
+    p.close()
+    # outer tile extent 16 > 8 falls back; the request "shared" holds across tilings
+    p = NFFT([32, 32, 32], precision="f32", device=dev).set_nodes(x3)
+    assert p.spread_kernel() == "register"
+    p.set_tiling([16])
+    assert p.spread_kernel() == "shared"
+    p.set_tiling([4])
+    assert p.spread_kernel() == "register"
+    p.set_spread_kernel("shared")
+    p.set_tiling([8])
+    assert p.spread_kernel() == "shared"
+    with pytest.raises(KeyError):
+        p.set_spread_kernel("bogus")
+    p.close()
+
+
+def test_autotune_picks_a_kernel_and_stays_correct(dev):
+    from cunfft_gb300.nfft import NFFT
+    rng = np.random.default_rng(21)
+    N, M = [32, 32, 32], 50000
+    x = rng.uniform(-0.5, 0.5, (M, 3))
+    f = _rand(M, rng)
+    p = NFFT(N, precision="f32", device=dev).set_nodes(torch.from_numpy(x).to(dev))
+    t = p.autotune(reps=1)
+    assert t["spread"] in ("register", "shared")
+    assert O.rel_l2(O.nfft_adjoint(x, f, N), p.adjoint(torch.from_numpy(f).to(dev)).cpu()) < TOL32
+    p.close()
