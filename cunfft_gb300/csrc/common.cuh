@@ -68,7 +68,7 @@ struct Tiling {
   int threads;           // CTA size of the gridding kernels
   size_t smem_tile;      // bytes of the staged tile
   int use_global;        // 1: no shared-memory tile fits, grid in global memory
-  int spread_reg;        // 1: spreading on the register-tile kernel (3D FP32, W <= 16, T0 <= 8)
+  int spread_kernel;     // spreading kernel in use: CUNFFT_X_SPREAD_SHARED, _REGISTER, _TENSOR or _GLOBAL
 };
 
 // Sorted node records, produced by the binning kernels.

@@ -123,6 +123,16 @@ static size_t smem_of(const Plan* p, const Tiling& tl) {
   return gridding_smem_bytes(q);
 }
 
+// Spreading kernel for the plan's current tiling under a request (plan_set_spread_kernel).
+static int pick_spread_kernel(const Plan& p, int mode) {
+  if (p.tl.use_global) return CUNFFT_X_SPREAD_GLOBAL;
+  const bool tc = spread_tc_supported(p), reg = spread_reg_supported(p);
+  if (mode == CUNFFT_X_SPREAD_TENSOR) return tc ? CUNFFT_X_SPREAD_TENSOR : CUNFFT_X_SPREAD_SHARED;
+  if (mode == CUNFFT_X_SPREAD_REGISTER) return reg ? CUNFFT_X_SPREAD_REGISTER : CUNFFT_X_SPREAD_SHARED;
+  if (mode == CUNFFT_X_SPREAD_SHARED) return CUNFFT_X_SPREAD_SHARED;
+  return tc ? CUNFFT_X_SPREAD_TENSOR : (reg ? CUNFFT_X_SPREAD_REGISTER : CUNFFT_X_SPREAD_SHARED);
+}
+
 // Tile extents: the caller's (or the defaults), clamped to the grid.  When the
 // padded tile does not fit in shared memory the largest extent is halved until it
 // does; when even 1-cell tiles do not fit (wide windows in 3D), the gridding runs
@@ -155,26 +165,27 @@ int plan_choose_tiling(Plan* p, const int* Tin, int chunk) {
   }
   if (tl.tiles_total >= (int64_t)1 << 31) return set_status(p, CUNFFT_X_INVALID_ARGUMENT, "too many tiles");
   p->tl = tl;
-  p->tl.spread_reg = p->spread_mode != CUNFFT_X_SPREAD_SHARED && spread_reg_supported(*p);
+  p->tl.spread_kernel = pick_spread_kernel(*p, p->spread_mode);
   p->bins.valid = 0;
   return CUNFFT_X_SUCCESS;
 }
 
-int plan_spread_kernel(const Plan* p) {
-  if (p->tl.use_global) return CUNFFT_X_SPREAD_GLOBAL;
-  return p->tl.spread_reg ? CUNFFT_X_SPREAD_REGISTER : CUNFFT_X_SPREAD_SHARED;
-}
+int plan_spread_kernel(const Plan* p) { return p->tl.spread_kernel; }
 
 // The kernel choice changes only the spreading launch, not the bins; captured
 // graphs are invalidated through node_gen.
 int plan_set_spread_kernel(Plan* p, int kind) {
-  if (kind != CUNFFT_X_SPREAD_AUTO && kind != CUNFFT_X_SPREAD_SHARED && kind != CUNFFT_X_SPREAD_REGISTER)
+  if (kind != CUNFFT_X_SPREAD_AUTO && kind != CUNFFT_X_SPREAD_SHARED && kind != CUNFFT_X_SPREAD_REGISTER &&
+      kind != CUNFFT_X_SPREAD_TENSOR)
     return set_status(p, CUNFFT_X_INVALID_ARGUMENT, "unknown spreading kernel %d", kind);
   if (kind == CUNFFT_X_SPREAD_REGISTER && !spread_reg_supported(*p))
     return set_status(p, CUNFFT_X_UNSUPPORTED,
                       "register spreading needs d = 3, FP32, 2m+2 <= 16 and an outer tile extent <= 8");
+  if (kind == CUNFFT_X_SPREAD_TENSOR && !spread_tc_supported(*p))
+    return set_status(p, CUNFFT_X_UNSUPPORTED,
+                      "tensor-core spreading needs d = 3, FP32, 2m+2 <= 16 and an outer tile extent <= 16");
   p->spread_mode = kind;
-  p->tl.spread_reg = kind != CUNFFT_X_SPREAD_SHARED && spread_reg_supported(*p);
+  p->tl.spread_kernel = pick_spread_kernel(*p, kind);
   ++p->node_gen;
   return set_status(p, CUNFFT_X_SUCCESS, nullptr);
 }
@@ -515,7 +526,7 @@ int plan_autotune(Plan* p, int reps) {
   const Tiling best0 = p->tl;
   float best = 3.0e38f;
   std::vector<int> best_T(3, 0);
-  int best_reg = 0;
+  int best_kind = 0;
   const size_t bytes = elem_bytes(p);
   void* scratch_f = nullptr;
   if (check_cuda(p, cudaMalloc(&scratch_f, bytes * std::max<int64_t>(p->M, 1)), "autotune scratch")) return p->last_status;
@@ -534,12 +545,17 @@ int plan_autotune(Plan* p, int reps) {
     if (!fits) continue;
     if (plan_choose_tiling(p, T, p->chunk_override) != CUNFFT_X_SUCCESS) continue;
     if (rebin(p) != CUNFFT_X_SUCCESS) break;
-    // both spreading kernels where the choice is open
-    std::vector<int> kinds{p->tl.spread_reg};
-    if (p->spread_mode == CUNFFT_X_SPREAD_AUTO && p->tl.spread_reg) kinds.push_back(0);
+    // every spreading kernel that covers the tiling, where the choice is open
+    std::vector<int> kinds{p->tl.spread_kernel};
+    if (p->spread_mode == CUNFFT_X_SPREAD_AUTO) {
+      if (p->tl.spread_kernel != CUNFFT_X_SPREAD_REGISTER && spread_reg_supported(*p))
+        kinds.push_back(CUNFFT_X_SPREAD_REGISTER);
+      if (p->tl.spread_kernel != CUNFFT_X_SPREAD_GLOBAL && p->tl.spread_kernel != CUNFFT_X_SPREAD_SHARED)
+        kinds.push_back(CUNFFT_X_SPREAD_SHARED);
+    }
     bool failed = false;
     for (int kind : kinds) {
-      p->tl.spread_reg = kind;
+      p->tl.spread_kernel = kind;
       // warm-up
       if (launch_interp(*p, p->g, scratch_f, p->stream) != cudaSuccess) continue;
       if (launch_spread(*p, scratch_f, p->g, p->stream) != cudaSuccess) continue;
@@ -558,7 +574,7 @@ int plan_autotune(Plan* p, int reps) {
       if (ms < best) {
         best = ms;
         best_T = {T[0], T[1], T[2]};
-        best_reg = kind;
+        best_kind = kind;
       }
     }
     if (failed) break;
@@ -575,7 +591,7 @@ int plan_autotune(Plan* p, int reps) {
   }
   int T[3] = {best_T[0], best_T[1], best_T[2]};
   CG_TRY(plan_choose_tiling(p, T, p->chunk_override));
-  p->tl.spread_reg = best_reg;
+  p->tl.spread_kernel = best_kind;
   CG_TRY(rebin(p));
   // the grid holds garbage from the timing runs; transforms rewrite it fully
   p->autotuned = true;

@@ -86,6 +86,10 @@ int plan_spread_kernel(const Plan* p);
 bool spread_reg_supported(const Plan& p);
 size_t spread_reg_smem_bytes(const Plan& p);
 cudaError_t grid_launch_spread_reg(const Plan& p, const void* f, void* g, cudaStream_t st);
+// tensor-core spreading kernel (grid_spread_tc.cu)
+bool spread_tc_supported(const Plan& p);
+size_t spread_tc_smem_bytes(const Plan& p);
+cudaError_t grid_launch_spread_tc(const Plan& p, const void* f, void* g, cudaStream_t st);
 
 // launchers (kernel .cu files); all asynchronous on st
 cudaError_t launch_binning(const Plan& p, const double* x, cudaStream_t st);

@@ -166,8 +166,21 @@ int cunfft_x_stage_times(cunfft_x_plan* h, double* t_bin, double* t_roc, double*
 
 int cunfft_x_synchronize(cunfft_x_plan* h) {
   if (!h) return CUNFFT_X_INVALID_ARGUMENT;
-  cudaError_t e = cudaStreamSynchronize(h->p.stream);
-  if (e != cudaSuccess) return cg::check_cuda(&h->p, e, "cudaStreamSynchronize");
+  cg::Plan& p = h->p;
+  cudaError_t e = cudaStreamSynchronize(p.stream);
+  if (e != cudaSuccess) return cg::check_cuda(&p, e, "cudaStreamSynchronize");
+  // device-side status: a bounded wait in a kernel that gave up (the flag is cleared on read)
+  int32_t flag = 0;
+  if (p.bins.status) {
+    e = cudaMemcpyAsync(&flag, p.bins.status, sizeof(flag), cudaMemcpyDeviceToHost, p.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(p.stream);
+    if (e != cudaSuccess) return cg::check_cuda(&p, e, "read device status");
+    if (flag != 0) {
+      cudaMemsetAsync(p.bins.status, 0, sizeof(int32_t), p.stream);
+      return cg::set_status(&p, CUNFFT_X_DEVICE_CHECK_FAILED,
+                            "device check failed (code %d): a tensor-core completion wait gave up", (int)flag);
+    }
+  }
   return CUNFFT_X_SUCCESS;
 }
 

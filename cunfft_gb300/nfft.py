@@ -176,14 +176,14 @@ class NFFT:
         nat.check(self._lib.cunfft_x_get_tiling(self._h, T, ctypes.byref(chunk), ctypes.byref(threads)))
         return {"T": list(T)[: self.d], "chunk": chunk.value, "threads": threads.value, "spread": self.spread_kernel()}
 
-    SPREAD_KERNELS = {"auto": 0, "shared": 1, "register": 2, "global": 3}
+    SPREAD_KERNELS = {"auto": 0, "shared": 1, "register": 2, "global": 3, "tensor": 4}
 
     def set_spread_kernel(self, kind="auto"):
-        """Request the spreading kernel: "auto", "shared" or "register"."""
+        """Request the spreading kernel: "auto", "shared", "register" or "tensor"."""
         nat.check(self._lib.cunfft_x_set_spread_kernel(self._h, self.SPREAD_KERNELS[kind]), self._h)
 
     def spread_kernel(self):
-        """Spreading kernel in use: "shared", "register" or "global"."""
+        """Spreading kernel in use: "shared", "register", "tensor" or "global"."""
         k = ctypes.c_int()
         nat.check(self._lib.cunfft_x_get_spread_kernel(self._h, ctypes.byref(k)))
         return {v: n for n, v in self.SPREAD_KERNELS.items()}[k.value]

@@ -28,14 +28,16 @@ extern "C" {
  *  FP32 keeps FP64 only for the node-to-grid reduction and the roll-off factors. */
 enum { CUNFFT_X_F64 = 0, CUNFFT_X_F32 = 1 };
 
-/** Spreading (adjoint gridding) kernel.  AUTO picks REGISTER where it applies
- *  (d = 3, FP32, 2m+2 <= 16, outer tile extent <= 8) and SHARED elsewhere;
- *  GLOBAL is reported when no shared-memory tile fits (wide 3D windows). */
+/** Spreading (adjoint gridding) kernel.  AUTO picks TENSOR where it applies
+ *  (d = 3, FP32, 2m+2 <= 16, outer tile extent <= 16), else REGISTER (same, outer
+ *  tile extent <= 8), else SHARED; GLOBAL is reported when no shared-memory tile
+ *  fits (wide 3D windows). */
 enum {
   CUNFFT_X_SPREAD_AUTO = 0,
   CUNFFT_X_SPREAD_SHARED = 1,   /* padded tile in shared memory, warp-owned planes */
   CUNFFT_X_SPREAD_REGISTER = 2, /* padded tile in registers, one warp per plane */
-  CUNFFT_X_SPREAD_GLOBAL = 3    /* atomics straight into the grid (fallback) */
+  CUNFFT_X_SPREAD_GLOBAL = 3,   /* atomics straight into the grid (fallback) */
+  CUNFFT_X_SPREAD_TENSOR = 4    /* tile update as 3xTF32 tcgen05 MMAs, tile in tensor memory */
 };
 
 /** Status codes returned by every cunfft_x_* entry point. */
@@ -151,19 +153,21 @@ int cunfft_x_autotune(cunfft_x_plan *plan, int reps);
 /** Current tiling: T[3], chunk, threads (any pointer may be NULL). */
 int cunfft_x_get_tiling(const cunfft_x_plan *plan, int *T, int *chunk, int *threads);
 
-/** Request a spreading kernel (CUNFFT_X_SPREAD_AUTO, _SHARED or _REGISTER).
- *  REGISTER on a plan it does not cover returns CUNFFT_X_UNSUPPORTED and keeps
- *  the current kernel.  The request holds across later tilings. */
+/** Request a spreading kernel (CUNFFT_X_SPREAD_AUTO, _SHARED, _REGISTER or
+ *  _TENSOR).  REGISTER or TENSOR on a plan they do not cover returns
+ *  CUNFFT_X_UNSUPPORTED and keeps the current kernel.  The request holds across
+ *  later tilings (a tiling the requested kernel does not cover runs SHARED). */
 int cunfft_x_set_spread_kernel(cunfft_x_plan *plan, int kind);
 
-/** Spreading kernel in use: CUNFFT_X_SPREAD_SHARED, _REGISTER or _GLOBAL. */
+/** Spreading kernel in use: CUNFFT_X_SPREAD_SHARED, _REGISTER, _TENSOR or _GLOBAL. */
 int cunfft_x_get_spread_kernel(const cunfft_x_plan *plan, int *kind);
 
 /** Per-stage device times of the last forward/adjoint call, in seconds
  *  (binning, roll-off, FFT, gridding).  Blocks until the plan stream is idle. */
 int cunfft_x_stage_times(cunfft_x_plan *plan, double *t_bin, double *t_roc, double *t_fft, double *t_conv);
 
-/** Block until the plan's stream is idle; reports asynchronous errors. */
+/** Block until the plan's stream is idle; reports asynchronous errors and
+ *  device-side check failures (CUNFFT_X_DEVICE_CHECK_FAILED, flag cleared on read). */
 int cunfft_x_synchronize(cunfft_x_plan *plan);
 
 /** Last error message of a plan (empty string when none). */

@@ -1,5 +1,5 @@
-"""Register-tile spreading kernel (3D FP32, 2m+2 <= 16) against the shared-tile
-kernel and the oracle; kernel selection through the extension API."""
+"""The 3D FP32 spreading kernels (tensor-core 3xTF32, register-tile, shared-tile)
+against each other and the oracle; kernel selection through the extension API."""
 import numpy as np
 import pytest
 
@@ -9,7 +9,7 @@ torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
 TOL32 = 1e-5     # FP32 form vs the FP64 oracle (relative l2), as the parity tests
-TOL_KERN = 2e-6  # the two FP32 spreading kernels against each other: summation order only
+TOL_KERN = 5e-6  # FP32 spreading kernels against each other (graph replay test)
 
 
 @pytest.fixture(scope="module")
@@ -23,33 +23,42 @@ def _rand(shape, rng):
     return rng.uniform(-1, 1, shape) + 1j * rng.uniform(-1, 1, shape)
 
 
-def _spread_both(p, f):
-    assert p.spread_kernel() == "register"
-    g_reg = p.spread(f).clone()
-    p.set_spread_kernel("shared")
-    assert p.spread_kernel() == "shared"
-    g_sh = p.spread(f).clone()
+def _spread_kinds(p, f, kinds):
+    """Grid of each requested spreading kernel (then back to the automatic choice)."""
+    out = {}
+    for k in kinds:
+        p.set_spread_kernel(k)
+        assert p.spread_kernel() == k
+        out[k] = p.spread(f).clone()
+        p.synchronize()  # raises on a device-side check failure
     p.set_spread_kernel("auto")
-    return g_reg, g_sh
+    return out
+
+
+def _agree(grids, ref, tol=TOL32):
+    """Every kernel's grid against the FP64 oracle grid."""
+    for k, g in grids.items():
+        err = O.rel_l2(ref, g.cpu().numpy())
+        assert err < tol, (k, err)
 
 
 @pytest.mark.parametrize("m", [1, 2, 3, 4, 5, 6, 7])
-def test_register_matches_shared_every_width(dev, m):
+def test_spread_kernels_agree_every_width(dev, m):
     from cunfft_gb300.nfft import NFFT
     rng = np.random.default_rng(100 + m)
     N, M = [32, 32, 32], 30000
     x = rng.uniform(-0.5, 0.5, (M, 3))
     f = _rand(M, rng)
     p = NFFT(N, m=m, precision="f32", device=dev).set_nodes(torch.from_numpy(x).to(dev))
+    assert p.spread_kernel() == "tensor"
     ft = torch.from_numpy(f).to(dev)
-    g_reg, g_sh = _spread_both(p, ft)
-    assert O.rel_l2(g_sh.cpu().numpy(), g_reg.cpu().numpy()) < TOL_KERN
+    _agree(_spread_kinds(p, ft, ["tensor", "register", "shared"]), O.spread(x, f, N, p.n, m))
     assert O.rel_l2(O.nfft_adjoint(x, f, N, m=m), p.adjoint(ft).cpu()) < TOL32
     p.close()
 
 
-@pytest.mark.parametrize("T0", [1, 2, 4, 8])
-def test_register_outer_tile_extents(dev, T0):
+@pytest.mark.parametrize("T0", [1, 2, 4, 8, 16])
+def test_spread_kernels_outer_tile_extents(dev, T0):
     from cunfft_gb300.nfft import NFFT
     rng = np.random.default_rng(7 + T0)
     N, M = [16, 32, 64], 20000
@@ -58,15 +67,16 @@ def test_register_outer_tile_extents(dev, T0):
     p = NFFT(N, m=6, precision="f32", device=dev).set_nodes(torch.from_numpy(x).to(dev))
     p.set_tiling([T0])
     assert p.tiling()["T"][0] == T0
-    g_reg, g_sh = _spread_both(p, torch.from_numpy(f).to(dev))
-    assert O.rel_l2(g_sh.cpu().numpy(), g_reg.cpu().numpy()) < TOL_KERN
+    kinds = ["tensor", "shared"] + (["register"] if T0 <= 8 else [])
+    ft = torch.from_numpy(f).to(dev)
+    _agree(_spread_kinds(p, ft, kinds), O.spread(x, f, N, p.n, 6))
+    assert O.rel_l2(O.nfft_adjoint(x, f, N), p.adjoint(ft).cpu()) < TOL32
     p.close()
 
 
 @pytest.mark.parametrize("N", [[4, 4, 4], [8, 2, 16], [2, 8, 4], [64, 8, 4]])
-def test_register_small_and_ragged_grids(dev, N):
-    """Grids smaller than the fixed inner tile (8 x 16): the padded tile wraps onto
-    itself and lane pairs straddle nothing."""
+def test_spread_kernels_small_and_ragged_grids(dev, N):
+    """Grids smaller than the fixed inner tile (8 x 16): the padded tile wraps onto itself."""
     from cunfft_gb300.nfft import NFFT
     rng = np.random.default_rng(sum(N))
     M = 3000
@@ -74,17 +84,17 @@ def test_register_small_and_ragged_grids(dev, N):
     f = _rand(M, rng)
     p = NFFT(N, m=3, precision="f32", device=dev).set_nodes(torch.from_numpy(x).to(dev))
     ft = torch.from_numpy(f).to(dev)
-    g_reg, g_sh = _spread_both(p, ft)
-    assert O.rel_l2(g_sh.cpu().numpy(), g_reg.cpu().numpy()) < TOL_KERN
+    _agree(_spread_kinds(p, ft, ["tensor", "register", "shared"]), O.spread(x, f, N, p.n, 3), 5 * TOL32)
     assert O.rel_l2(O.nfft_adjoint(x, f, N, m=3), p.adjoint(ft).cpu()) < 5 * TOL32
     p.close()
 
 
-def test_register_clustered_and_boundary_nodes(dev):
-    """Many nodes in a few tiles (long work-item chains), nodes on -1/2 and near +1/2."""
+def test_spread_kernels_clustered_and_boundary_nodes(dev):
+    """Many nodes in a few tiles (long work-item chains, partial batches), nodes on -1/2,
+    just below +1/2 and at -0.0."""
     from cunfft_gb300.nfft import NFFT
     rng = np.random.default_rng(5)
-    N, M = [32, 32, 32], 40000
+    N, M = [32, 32, 32], 40001
     x = np.clip(rng.normal(0.1, 0.02, (M, 3)), -0.5, 0.4999)
     x[:50] = -0.5
     x[50:100] = np.nextafter(0.5, 0)
@@ -92,13 +102,12 @@ def test_register_clustered_and_boundary_nodes(dev):
     f = _rand(M, rng)
     p = NFFT(N, m=6, precision="f32", device=dev).set_nodes(torch.from_numpy(x).to(dev))
     ft = torch.from_numpy(f).to(dev)
-    g_reg, g_sh = _spread_both(p, ft)
-    assert O.rel_l2(g_sh.cpu().numpy(), g_reg.cpu().numpy()) < TOL_KERN
+    _agree(_spread_kinds(p, ft, ["tensor", "register", "shared"]), O.spread(x, f, N, p.n, 6))
     assert O.rel_l2(O.nfft_adjoint(x, f, N), p.adjoint(ft).cpu()) < TOL32
     p.close()
 
 
-def test_register_batched_uneven(dev):
+def test_spread_kernels_batched_uneven(dev):
     from cunfft_gb300.nfft import NFFT
     rng = np.random.default_rng(11)
     N, Ms = [16, 16, 16], [5000, 0, 1234]
@@ -107,8 +116,8 @@ def test_register_batched_uneven(dev):
     p = NFFT(N, m=5, precision="f32", batch=3, device=dev)
     p.set_nodes(torch.from_numpy(np.concatenate(xs)).to(dev), M_inst=Ms)
     ft = torch.from_numpy(np.concatenate(fs)).to(dev)
-    g_reg, g_sh = _spread_both(p, ft)
-    assert O.rel_l2(g_sh.cpu().numpy(), g_reg.cpu().numpy()) < TOL_KERN
+    ref = np.stack([O.spread(xs[i], fs[i], N, p.n, 5) for i in range(3)])
+    _agree(_spread_kinds(p, ft, ["tensor", "register", "shared"]), ref)
     got = p.adjoint(ft).cpu().numpy()
     for i in range(3):
         if Ms[i]:
@@ -118,7 +127,22 @@ def test_register_batched_uneven(dev):
     p.close()
 
 
-def test_register_graph_follows_kernel_choice(dev):
+def test_spread_tensor_few_nodes(dev):
+    """1, 7 and 17 nodes: partial batches of the 16-node staging."""
+    from cunfft_gb300.nfft import NFFT
+    rng = np.random.default_rng(13)
+    N = [16, 16, 16]
+    for M in (1, 7, 17):
+        x = rng.uniform(-0.5, 0.5, (M, 3))
+        f = _rand(M, rng)
+        p = NFFT(N, precision="f32", device=dev).set_nodes(torch.from_numpy(x).to(dev))
+        ft = torch.from_numpy(f).to(dev)
+        _agree(_spread_kinds(p, ft, ["tensor", "shared"]), O.spread(x, f, N, p.n, 6))
+        assert O.rel_l2(O.nfft_adjoint(x, f, N), p.adjoint(ft).cpu()) < TOL32
+        p.close()
+
+
+def test_spread_kernel_graph_follows_choice(dev):
     from cunfft_gb300.nfft import NFFT
     rng = np.random.default_rng(12)
     N, M = [32, 32, 32], 20000
@@ -126,43 +150,47 @@ def test_register_graph_follows_kernel_choice(dev):
     f = torch.from_numpy(_rand(M, rng)).to(dev).to(torch.complex64)
     p = NFFT(N, precision="f32", device=dev).set_nodes(torch.from_numpy(x).to(dev))
     out = torch.empty(N, dtype=torch.complex64, device=dev)
-    p.adjoint_graph(f, out)
-    a = out.clone()
-    p.set_spread_kernel("shared")
-    p.adjoint_graph(f, out)
-    b = out.clone()
+    outs = {}
+    for k in ("tensor", "register", "shared"):
+        p.set_spread_kernel(k)
+        p.adjoint_graph(f, out)
+        outs[k] = out.clone()
     torch.cuda.synchronize()
-    assert O.rel_l2(a.cpu().numpy(), b.cpu().numpy()) < TOL_KERN
-    assert O.rel_l2(p.adjoint(f).cpu().numpy(), b.cpu().numpy()) < TOL_KERN
+    ref = p.adjoint(f).cpu().numpy()
+    for k, v in outs.items():
+        assert O.rel_l2(ref, v.cpu().numpy()) < TOL_KERN, k
     p.close()
 
 
-def test_kernel_selection_rules(dev):
+def test_spread_kernel_selection_rules(dev):
     from cunfft_gb300._native import CunfftError
     from cunfft_gb300.nfft import NFFT
     x3 = torch.rand(100, 3, dtype=torch.float64, device=dev) - 0.5
-    # FP64 and 2D plans: the register kernel does not apply
-    p = NFFT([16, 16, 16], precision="f64", device=dev).set_nodes(x3)
-    assert p.spread_kernel() == "shared"
-    with pytest.raises(CunfftError):
-        p.set_spread_kernel("register")
-    p.close()
-    p = NFFT([32, 32], precision="f32", device=dev).set_nodes(x3[:, :2].contiguous())
-    assert p.spread_kernel() == "shared"
-    with pytest.raises(CunfftError):
-        p.set_spread_kernel("register")
-    p.close()
-    # W = 18 > 16
+    # FP64 and 2D plans: only the shared-tile kernel
+    for prec, N, x in (("f64", [16, 16, 16], x3), ("f32", [32, 32], x3[:, :2].contiguous())):
+        p = NFFT(N, precision=prec, device=dev).set_nodes(x)
+        assert p.spread_kernel() == "shared"
+        for k in ("register", "tensor"):
+            with pytest.raises(CunfftError):
+                p.set_spread_kernel(k)
+        assert p.spread_kernel() == "shared"
+        p.close()
+    # 2m+2 = 18 > 16
     p = NFFT([16, 16, 16], m=8, precision="f32", device=dev).set_nodes(x3)
     assert p.spread_kernel() == "shared"
     p.close()
-    # outer tile extent 16 > 8 falls back; the request "shared" holds across tilings
     p = NFFT([32, 32, 32], precision="f32", device=dev).set_nodes(x3)
+    assert p.spread_kernel() == "tensor"
+    p.set_spread_kernel("register")
     assert p.spread_kernel() == "register"
-    p.set_tiling([16])
+    p.set_tiling([16])                  # the register kernel stops at 8: shared, request kept
     assert p.spread_kernel() == "shared"
     p.set_tiling([4])
     assert p.spread_kernel() == "register"
+    p.set_spread_kernel("auto")
+    assert p.spread_kernel() == "tensor"
+    p.set_tiling([16])
+    assert p.spread_kernel() == "tensor"
     p.set_spread_kernel("shared")
     p.set_tiling([8])
     assert p.spread_kernel() == "shared"
@@ -179,6 +207,7 @@ def test_autotune_picks_a_kernel_and_stays_correct(dev):
     f = _rand(M, rng)
     p = NFFT(N, precision="f32", device=dev).set_nodes(torch.from_numpy(x).to(dev))
     t = p.autotune(reps=1)
-    assert t["spread"] in ("register", "shared")
+    assert t["spread"] in ("tensor", "register", "shared")
     assert O.rel_l2(O.nfft_adjoint(x, f, N), p.adjoint(torch.from_numpy(f).to(dev)).cpu()) < TOL32
+    p.synchronize()
     p.close()
