@@ -83,6 +83,7 @@ struct Bins {
   int32_t* num_items;    // [1]
   int32_t* work;         // [2] persistent work-queue counters (forward, adjoint)
   int2*    tile_rank;    // [M] per node (tile, rank) scratch
+  void*    fperm;        // [M] complex: the samples in sorted order (filled per call by the tensor-core spreading)
   int32_t* inst_off;     // [batch + 1] node offsets per instance
   int32_t* status;       // [1] device-side error flag
   int64_t  M;            // total nodes

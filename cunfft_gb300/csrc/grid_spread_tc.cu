@@ -1,4 +1,6 @@
 // grid_spread_tc.cu -- launcher of the tensor-core 3D FP32 spreading kernel.
+#include <algorithm>
+
 #include "kernels_spread_tc.cuh"
 
 namespace cg {
@@ -13,7 +15,7 @@ bool spread_tc_supported(const Plan& p) {
 // the SM's 512 tensor-memory columns and tcgen05.alloc never waits.
 static constexpr size_t kSmemPerSm = 228u * 1024u;  // per SM; each resident CTA also reserves 1 KB
 size_t spread_tc_smem_bytes(const Plan& p) {
-  const TcLayout L = tc_layout(p.geo.W, p.tl.E[0], p.tl.smem_tile);
+  const TcLayout L = tc_layout(p.geo.W, p.tl.E[0]);
   const size_t k = 512u / L.tmem_cols;
   const size_t floor_bytes = kSmemPerSm / (k + 1) + 1;  // k + 1 CTAs of this size exceed the SM
   return L.total > floor_bytes ? L.total : floor_bytes;
@@ -30,7 +32,11 @@ static cudaError_t launch_tc(const Plan& p, const void* in, void* out, cudaStrea
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kTcThreads, smem);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
-  if ((size_t)per_sm * tc_layout(W, p.tl.E[0], p.tl.smem_tile).tmem_cols > 512u) return cudaErrorInvalidConfiguration;
+  if ((size_t)per_sm * tc_layout(W, p.tl.E[0]).tmem_cols > 512u) return cudaErrorInvalidConfiguration;
+  // samples in sorted order, read contiguously by the kernel's record loads
+  const int64_t M = p.bins.M;
+  const int pblocks = (int)std::min<int64_t>((M + 255) / 256, (int64_t)p.num_sms * 16);
+  k_permute_samples<<<pblocks, 256, 0, st>>>((const float2*)in, p.bins.sidx, M, (float2*)p.bins.fperm);
   kern<<<p.num_sms * per_sm, kTcThreads, smem, st>>>((const float2*)in, (float2*)out, p.geo, p.tl, p.bins);
   return cudaGetLastError();
 }

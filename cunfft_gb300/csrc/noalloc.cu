@@ -10,7 +10,7 @@
 // file-scope device array instead of plan-owned allocations.
 //
 // That array is part of the library's device image: every GPU on which the
-// library is loaded holds it (about 42 MB) until the process exits.  All calls
+// library is loaded holds it (about 58 MB) until the process exits.  All calls
 // share it, so calls that overlap on the GPU (concurrent streams, or host
 // threads driving the same device) race on it and must be serialised by the
 // caller.  Every call rewrites all scratch it reads: the per-tile counts and the
@@ -34,7 +34,8 @@ constexpr size_t kOffSidx = 0;
 constexpr size_t kOffSoff = na_align(kOffSidx + sizeof(int32_t) * kNaMaxNodes);
 constexpr size_t kOffSfrac = na_align(kOffSoff + sizeof(int32_t) * kNaMaxNodes);
 constexpr size_t kOffRank = na_align(kOffSfrac + sizeof(double) * 3 * kNaMaxNodes);
-constexpr size_t kOffCount = na_align(kOffRank + sizeof(int2) * kNaMaxNodes);
+constexpr size_t kOffFperm = na_align(kOffRank + sizeof(int2) * kNaMaxNodes);
+constexpr size_t kOffCount = na_align(kOffFperm + sizeof(double) * 2 * kNaMaxNodes);
 constexpr size_t kOffTileOff = na_align(kOffCount + sizeof(int32_t) * (kNaMaxTiles + 1));
 constexpr size_t kOffItemOff = na_align(kOffTileOff + sizeof(int32_t) * (kNaMaxTiles + 1));
 constexpr size_t kOffItems = na_align(kOffItemOff + sizeof(int32_t) * (kNaMaxTiles + 1));
@@ -117,6 +118,7 @@ extern "C" int cunfft_x_spread_noalloc(int d, const int64_t* N, const int64_t* n
   B.soff = reinterpret_cast<int32_t*>(base + kOffSoff);
   B.sfrac = base + kOffSfrac;
   B.tile_rank = reinterpret_cast<int2*>(base + kOffRank);
+  B.fperm = base + kOffFperm;
   B.count = reinterpret_cast<int32_t*>(base + kOffCount);
   B.tile_off = reinterpret_cast<int32_t*>(base + kOffTileOff);
   B.item_off = reinterpret_cast<int32_t*>(base + kOffItemOff);

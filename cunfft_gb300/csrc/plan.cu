@@ -59,12 +59,13 @@ static void free_bins(Plan* p) {
   cudaFree(B.sidx);
   cudaFree(B.soff);
   cudaFree(B.sfrac);
+  cudaFree(B.fperm);
   cudaFree(B.tile_rank);
   cudaFree(B.count);
   cudaFree(B.tile_off);
   cudaFree(B.item_off);
   cudaFree(B.items);
-  B.sidx = nullptr; B.soff = nullptr; B.sfrac = nullptr; B.tile_rank = nullptr;
+  B.sidx = nullptr; B.soff = nullptr; B.sfrac = nullptr; B.tile_rank = nullptr; B.fperm = nullptr;
   B.count = nullptr; B.tile_off = nullptr; B.item_off = nullptr; B.items = nullptr;
   p->bins_capacity_M = -1;
   p->bins_capacity_tiles = -1;
@@ -348,6 +349,7 @@ static int ensure_bins(Plan* p, int64_t M) {
     CG_TRY(check_cuda(p, cudaMalloc(&B.soff, sizeof(int32_t) * capM), "cudaMalloc bins"));
     CG_TRY(check_cuda(p, cudaMalloc(&B.sfrac, real * p->geo.d * capM), "cudaMalloc bins"));
     CG_TRY(check_cuda(p, cudaMalloc(&B.tile_rank, sizeof(int2) * capM), "cudaMalloc bins"));
+    CG_TRY(check_cuda(p, cudaMalloc(&B.fperm, elem_bytes(p) * capM), "cudaMalloc bins"));
     CG_TRY(check_cuda(p, cudaMalloc(&B.count, sizeof(int32_t) * (capT + 1)), "cudaMalloc bins"));
     CG_TRY(check_cuda(p, cudaMalloc(&B.tile_off, sizeof(int32_t) * (capT + 1)), "cudaMalloc bins"));
     CG_TRY(check_cuda(p, cudaMalloc(&B.item_off, sizeof(int32_t) * (capT + 1)), "cudaMalloc bins"));

@@ -125,7 +125,7 @@ int cunfft_x_spread(cunfft_x_plan *plan, const void *f, void *g);
  *  (n_t = 2*next_pow2(N_t)).
  *
  *  Its scratch (node bins, tile counts, work queue) is one fixed device array
- *  inside the library, about 42 MB, which every GPU that loads the library holds
+ *  inside the library, about 58 MB, which every GPU that loads the library holds
  *  until the process exits.  Limits: M <= 1048576 nodes and at most 65536 grid
  *  tiles (every 3D grid up to 256^3 and every 2D grid up to 8192^2 fits); larger
  *  requests return
