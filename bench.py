@@ -400,7 +400,9 @@ def run_ours(args):
                 "d2h_bytes_per_step": d2h, "ms_per_step": ms_e2e,
                 "path": "cunfft_x C ABI, pinned host buffers, copies on the plan stream"},
         "roofline": roofline,
-        "gpu_launches": args.steps * 8,
+        # binning 4 (count, scan, scatter, items) + forward 2 (roll-off, interpolation)
+        # + adjoint 2 (spreading, roll-off) + the sample permutation of the tensor-core spreading
+        "gpu_launches": args.steps * (8 + (1 if p32.spread_kernel() == "tensor" else 0)),
         "clocks": clk,
     }
     if cpu is not None:

@@ -69,6 +69,7 @@ struct Tiling {
   size_t smem_tile;      // bytes of the staged tile
   int use_global;        // 1: no shared-memory tile fits, grid in global memory
   int spread_kernel;     // spreading kernel in use: CUNFFT_X_SPREAD_SHARED, _REGISTER, _TENSOR or _GLOBAL
+  int interp_kernel;     // interpolation kernel in use: CUNFFT_X_INTERP_SHARED, _TENSOR or _GLOBAL
 };
 
 // Sorted node records, produced by the binning kernels.

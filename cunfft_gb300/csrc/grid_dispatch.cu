@@ -25,6 +25,7 @@ cudaError_t grid_launch_global(const Plan&, bool, const void*, void*, cudaStream
 static cudaError_t dispatch(const Plan& p, bool spread, const void* in, void* out, cudaStream_t st) {
   if (p.tl.use_global) return grid_launch_global(p, spread, in, out, st);
   if (spread && p.tl.spread_kernel == CUNFFT_X_SPREAD_TENSOR) return grid_launch_spread_tc(p, in, out, st);
+  if (!spread && p.tl.interp_kernel == CUNFFT_X_INTERP_TENSOR) return grid_launch_interp_tc(p, in, out, st);
   if (spread && p.tl.spread_kernel == CUNFFT_X_SPREAD_REGISTER) return grid_launch_spread_reg(p, in, out, st);
   switch (p.geo.W) {
 #define CG_CASE(W) case W: return grid_launch_w##W(p, spread, in, out, st);

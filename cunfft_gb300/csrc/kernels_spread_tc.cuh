@@ -103,22 +103,6 @@ __device__ __forceinline__ uint32_t tc_elem_off(int rg, int ri, int kg) {
   return (uint32_t)rg * kTcSBO + (uint32_t)kg * kTcLBO + (uint32_t)ri * 16u;
 }
 
-__device__ __forceinline__ void tc_split4(float4 v, float4& hi, float4& lo) {
-  hi.x = tc::tf32_round(v.x);
-  hi.y = tc::tf32_round(v.y);
-  hi.z = tc::tf32_round(v.z);
-  hi.w = tc::tf32_round(v.w);
-  lo.x = v.x - hi.x;
-  lo.y = v.y - hi.y;
-  lo.z = v.z - hi.z;
-  lo.w = v.w - hi.w;
-}
-
-// tap weight exp(-(fr + m - l)^2 / b) (as WeightMath<float>::taps), zero outside the window
-__device__ __forceinline__ float tc_tap(float fr, float mf, int l, int W, float cb) {
-  const float y = fr + (mf - (float)l);
-  return (unsigned)l < (unsigned)W ? exp2f(-(y * y) * cb) : 0.f;
-}
 
 // Position in this CTA's batch sequence: work items c, c + G, c + 2G, ... (CTA c,
 // G CTAs; items are never empty) and the batch of kTcK nodes within the item.

@@ -134,6 +134,13 @@ static int pick_spread_kernel(const Plan& p, int mode) {
   return tc ? CUNFFT_X_SPREAD_TENSOR : (reg ? CUNFFT_X_SPREAD_REGISTER : CUNFFT_X_SPREAD_SHARED);
 }
 
+// Interpolation kernel for the plan's current tiling under a request (plan_set_interp_kernel).
+static int pick_interp_kernel(const Plan& p, int mode) {
+  if (p.tl.use_global) return CUNFFT_X_INTERP_GLOBAL;
+  if (mode == CUNFFT_X_INTERP_SHARED) return CUNFFT_X_INTERP_SHARED;
+  return interp_tc_supported(p) ? CUNFFT_X_INTERP_TENSOR : CUNFFT_X_INTERP_SHARED;
+}
+
 // Tile extents: the caller's (or the defaults), clamped to the grid.  When the
 // padded tile does not fit in shared memory the largest extent is halved until it
 // does; when even 1-cell tiles do not fit (wide windows in 3D), the gridding runs
@@ -167,8 +174,23 @@ int plan_choose_tiling(Plan* p, const int* Tin, int chunk) {
   if (tl.tiles_total >= (int64_t)1 << 31) return set_status(p, CUNFFT_X_INVALID_ARGUMENT, "too many tiles");
   p->tl = tl;
   p->tl.spread_kernel = pick_spread_kernel(*p, p->spread_mode);
+  p->tl.interp_kernel = pick_interp_kernel(*p, p->interp_mode);
   p->bins.valid = 0;
   return CUNFFT_X_SUCCESS;
+}
+
+int plan_interp_kernel(const Plan* p) { return p->tl.interp_kernel; }
+
+int plan_set_interp_kernel(Plan* p, int kind) {
+  if (kind != CUNFFT_X_INTERP_AUTO && kind != CUNFFT_X_INTERP_SHARED && kind != CUNFFT_X_INTERP_TENSOR)
+    return set_status(p, CUNFFT_X_INVALID_ARGUMENT, "unknown interpolation kernel %d", kind);
+  if (kind == CUNFFT_X_INTERP_TENSOR && !interp_tc_supported(*p))
+    return set_status(p, CUNFFT_X_UNSUPPORTED,
+                      "tensor-core interpolation needs d = 3, FP32, 2m+2 <= 16, an outer tile extent <= 16 and n_3 >= 4");
+  p->interp_mode = kind;
+  p->tl.interp_kernel = pick_interp_kernel(*p, kind);
+  ++p->node_gen;
+  return set_status(p, CUNFFT_X_SUCCESS, nullptr);
 }
 
 int plan_spread_kernel(const Plan* p) { return p->tl.spread_kernel; }
@@ -509,10 +531,10 @@ int plan_node_gradient(Plan* p, const void* fhat, const void* grad_f, double* gr
   return set_status(p, CUNFFT_X_SUCCESS, nullptr);
 }
 
-// Autotuner: time interpolation and spreading for a few tilings on the bound
-// node set (and, where the register-tile spreading kernel applies and no kernel
-// was requested, both spreading kernels); keep the fastest sum.  Restores the
-// previous tiling when a candidate fails.
+// Autotuner: time interpolation and spreading for a few tilings on the bound node
+// set, each with every kernel that covers the tiling where no kernel was requested;
+// keep the tiling with the fastest sum of the fastest kernels.  Restores the
+// previous tiling when no candidate runs.
 int plan_autotune(Plan* p, int reps) {
   if (!p->nodes_set) return set_status(p, CUNFFT_X_NODES_NOT_SET, "autotune: nodes not set");
   if (reps < 1) reps = 1;
@@ -528,7 +550,7 @@ int plan_autotune(Plan* p, int reps) {
   const Tiling best0 = p->tl;
   float best = 3.0e38f;
   std::vector<int> best_T(3, 0);
-  int best_kind = 0;
+  int best_sk = 0, best_ik = 0;
   const size_t bytes = elem_bytes(p);
   void* scratch_f = nullptr;
   if (check_cuda(p, cudaMalloc(&scratch_f, bytes * std::max<int64_t>(p->M, 1)), "autotune scratch")) return p->last_status;
@@ -540,6 +562,24 @@ int plan_autotune(Plan* p, int reps) {
   cudaEventCreate(&b);
   const bool timing = p->timing;
   p->timing = false;
+  bool failed = false;
+  // device time of reps launches of one gridding kernel (after one warm-up); < 0 on failure
+  auto time_kernel = [&](bool spread) -> float {
+    auto run = [&]() {
+      return spread ? launch_spread(*p, scratch_f, p->g, p->stream) : launch_interp(*p, p->g, scratch_f, p->stream);
+    };
+    if (run() != cudaSuccess) return -1.f;
+    cudaEventRecord(a, p->stream);
+    for (int r = 0; r < reps; ++r) run();
+    cudaEventRecord(b, p->stream);
+    if (cudaEventSynchronize(b) != cudaSuccess) {
+      failed = true;
+      return -1.f;
+    }
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    return ms;
+  };
   for (auto& c : cands) {
     int T[3] = {c[0], c[1], c[2]};
     bool fits = true;
@@ -547,39 +587,44 @@ int plan_autotune(Plan* p, int reps) {
     if (!fits) continue;
     if (plan_choose_tiling(p, T, p->chunk_override) != CUNFFT_X_SUCCESS) continue;
     if (rebin(p) != CUNFFT_X_SUCCESS) break;
-    // every spreading kernel that covers the tiling, where the choice is open
-    std::vector<int> kinds{p->tl.spread_kernel};
+    // every kernel that covers the tiling, where the choice is open; interpolation
+    // and spreading are timed separately and the fastest of each kept
+    std::vector<int> skinds{p->tl.spread_kernel}, ikinds{p->tl.interp_kernel};
     if (p->spread_mode == CUNFFT_X_SPREAD_AUTO) {
       if (p->tl.spread_kernel != CUNFFT_X_SPREAD_REGISTER && spread_reg_supported(*p))
-        kinds.push_back(CUNFFT_X_SPREAD_REGISTER);
+        skinds.push_back(CUNFFT_X_SPREAD_REGISTER);
       if (p->tl.spread_kernel != CUNFFT_X_SPREAD_GLOBAL && p->tl.spread_kernel != CUNFFT_X_SPREAD_SHARED)
-        kinds.push_back(CUNFFT_X_SPREAD_SHARED);
+        skinds.push_back(CUNFFT_X_SPREAD_SHARED);
     }
-    bool failed = false;
-    for (int kind : kinds) {
+    if (p->interp_mode == CUNFFT_X_INTERP_AUTO && p->tl.interp_kernel == CUNFFT_X_INTERP_TENSOR)
+      ikinds.push_back(CUNFFT_X_INTERP_SHARED);
+    float bs = 3.0e38f, bi = 3.0e38f;
+    int sk = skinds[0], ik = ikinds[0];
+    for (int kind : skinds) {
       p->tl.spread_kernel = kind;
-      // warm-up
-      if (launch_interp(*p, p->g, scratch_f, p->stream) != cudaSuccess) continue;
-      if (launch_spread(*p, scratch_f, p->g, p->stream) != cudaSuccess) continue;
-      cudaEventRecord(a, p->stream);
-      for (int r = 0; r < reps; ++r) {
-        launch_interp(*p, p->g, scratch_f, p->stream);
-        launch_spread(*p, scratch_f, p->g, p->stream);
+      const float ms = time_kernel(true);
+      if (failed) break;
+      if (ms >= 0.f && ms < bs) {
+        bs = ms;
+        sk = kind;
       }
-      cudaEventRecord(b, p->stream);
-      if (cudaEventSynchronize(b) != cudaSuccess) {
-        failed = true;
-        break;
-      }
-      float ms = 0;
-      cudaEventElapsedTime(&ms, a, b);
-      if (ms < best) {
-        best = ms;
-        best_T = {T[0], T[1], T[2]};
-        best_kind = kind;
+    }
+    for (int kind : ikinds) {
+      if (failed) break;
+      p->tl.interp_kernel = kind;
+      const float ms = time_kernel(false);
+      if (ms >= 0.f && ms < bi) {
+        bi = ms;
+        ik = kind;
       }
     }
     if (failed) break;
+    if (bs < 3.0e38f && bi < 3.0e38f && bs + bi < best) {
+      best = bs + bi;
+      best_T = {T[0], T[1], T[2]};
+      best_sk = sk;
+      best_ik = ik;
+    }
   }
   p->timing = timing;
   cudaEventDestroy(a);
@@ -593,7 +638,8 @@ int plan_autotune(Plan* p, int reps) {
   }
   int T[3] = {best_T[0], best_T[1], best_T[2]};
   CG_TRY(plan_choose_tiling(p, T, p->chunk_override));
-  p->tl.spread_kernel = best_kind;
+  p->tl.spread_kernel = best_sk;
+  p->tl.interp_kernel = best_ik;
   CG_TRY(rebin(p));
   // the grid holds garbage from the timing runs; transforms rewrite it fully
   p->autotuned = true;

@@ -43,6 +43,7 @@ struct Plan {
   int tile_override[kMaxDim] = {0, 0, 0};
   int chunk_override = 0;
   int spread_mode = CUNFFT_X_SPREAD_AUTO;  // requested spreading kernel
+  int interp_mode = CUNFFT_X_INTERP_AUTO;  // requested interpolation kernel
   bool autotuned = false;
   int last_status = 0;
   char last_msg[256] = {0};
@@ -81,6 +82,8 @@ int plan_choose_tiling(Plan* p, const int* T, int chunk);
 int plan_autotune(Plan* p, int reps);
 int plan_set_spread_kernel(Plan* p, int kind);
 int plan_spread_kernel(const Plan* p);
+int plan_set_interp_kernel(Plan* p, int kind);
+int plan_interp_kernel(const Plan* p);
 
 // register-tile spreading kernel (grid_spread_reg.cu)
 bool spread_reg_supported(const Plan& p);
@@ -90,6 +93,9 @@ cudaError_t grid_launch_spread_reg(const Plan& p, const void* f, void* g, cudaSt
 bool spread_tc_supported(const Plan& p);
 size_t spread_tc_smem_bytes(const Plan& p);
 cudaError_t grid_launch_spread_tc(const Plan& p, const void* f, void* g, cudaStream_t st);
+// tensor-core interpolation kernel (grid_interp_tc.cu)
+bool interp_tc_supported(const Plan& p);
+cudaError_t grid_launch_interp_tc(const Plan& p, const void* g, void* f, cudaStream_t st);
 
 // launchers (kernel .cu files); all asynchronous on st
 cudaError_t launch_binning(const Plan& p, const double* x, cudaStream_t st);

@@ -135,4 +135,24 @@ __device__ __forceinline__ float tf32_round(float v) {
 }
 
 }  // namespace tc
+
+// (hi, lo) 3xTF32 parts of four values
+__device__ __forceinline__ void tc_split4(float4 v, float4& hi, float4& lo) {
+  hi.x = tc::tf32_round(v.x);
+  hi.y = tc::tf32_round(v.y);
+  hi.z = tc::tf32_round(v.z);
+  hi.w = tc::tf32_round(v.w);
+  lo.x = v.x - hi.x;
+  lo.y = v.y - hi.y;
+  lo.z = v.z - hi.z;
+  lo.w = v.w - hi.w;
+}
+
+// Gaussian tap exp(-(fr + m - l)^2 / b) = exp2(-(fr + m - l)^2 cb), the FP32 tap of
+// WeightMath<float>::taps (cb = log2(e) / b), zero outside the window 0 <= l < W
+__device__ __forceinline__ float tc_tap(float fr, float mf, int l, int W, float cb) {
+  const float y = fr + (mf - (float)l);
+  return (unsigned)l < (unsigned)W ? exp2f(-(y * y) * cb) : 0.f;
+}
+
 }  // namespace cg

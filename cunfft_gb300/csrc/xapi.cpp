@@ -141,6 +141,17 @@ int cunfft_x_get_spread_kernel(const cunfft_x_plan* h, int* kind) {
   return CUNFFT_X_SUCCESS;
 }
 
+int cunfft_x_set_interp_kernel(cunfft_x_plan* h, int kind) {
+  if (!h) return CUNFFT_X_INVALID_ARGUMENT;
+  return cg::plan_set_interp_kernel(&h->p, kind);
+}
+
+int cunfft_x_get_interp_kernel(const cunfft_x_plan* h, int* kind) {
+  if (!h || !kind) return CUNFFT_X_INVALID_ARGUMENT;
+  *kind = cg::plan_interp_kernel(&h->p);
+  return CUNFFT_X_SUCCESS;
+}
+
 static double ev_seconds(cudaEvent_t a, cudaEvent_t b) {
   float ms = 0.0f;
   if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) {

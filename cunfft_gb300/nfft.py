@@ -174,7 +174,8 @@ class NFFT:
         T = (ctypes.c_int * 3)()
         chunk, threads = ctypes.c_int(), ctypes.c_int()
         nat.check(self._lib.cunfft_x_get_tiling(self._h, T, ctypes.byref(chunk), ctypes.byref(threads)))
-        return {"T": list(T)[: self.d], "chunk": chunk.value, "threads": threads.value, "spread": self.spread_kernel()}
+        return {"T": list(T)[: self.d], "chunk": chunk.value, "threads": threads.value, "spread": self.spread_kernel(),
+                "interp": self.interp_kernel()}
 
     SPREAD_KERNELS = {"auto": 0, "shared": 1, "register": 2, "global": 3, "tensor": 4}
 
@@ -187,6 +188,18 @@ class NFFT:
         k = ctypes.c_int()
         nat.check(self._lib.cunfft_x_get_spread_kernel(self._h, ctypes.byref(k)))
         return {v: n for n, v in self.SPREAD_KERNELS.items()}[k.value]
+
+    INTERP_KERNELS = {"auto": 0, "shared": 1, "global": 3, "tensor": 4}
+
+    def set_interp_kernel(self, kind="auto"):
+        """Request the interpolation kernel: "auto", "shared" or "tensor"."""
+        nat.check(self._lib.cunfft_x_set_interp_kernel(self._h, self.INTERP_KERNELS[kind]), self._h)
+
+    def interp_kernel(self):
+        """Interpolation kernel in use: "shared", "tensor" or "global"."""
+        k = ctypes.c_int()
+        nat.check(self._lib.cunfft_x_get_interp_kernel(self._h, ctypes.byref(k)))
+        return {v: n for n, v in self.INTERP_KERNELS.items()}[k.value]
 
     def autotune(self, reps=3):
         nat.check(self._lib.cunfft_x_autotune(self._h, int(reps)), self._h)

@@ -40,6 +40,16 @@ enum {
   CUNFFT_X_SPREAD_TENSOR = 4    /* tile update as 3xTF32 tcgen05 MMAs, tile in tensor memory */
 };
 
+/** Interpolation (forward gridding) kernel.  AUTO picks TENSOR where it applies
+ *  (d = 3, FP32, 2m+2 <= 16, outer tile extent <= 16, n_3 >= 4) and SHARED
+ *  elsewhere; GLOBAL is reported when no shared-memory tile fits. */
+enum {
+  CUNFFT_X_INTERP_AUTO = 0,
+  CUNFFT_X_INTERP_SHARED = 1,   /* tile staged in shared memory, warp per node */
+  CUNFFT_X_INTERP_GLOBAL = 3,   /* taps read straight from the grid (fallback) */
+  CUNFFT_X_INTERP_TENSOR = 4    /* innermost contraction as 3xTF32 tcgen05 MMAs */
+};
+
 /** Status codes returned by every cunfft_x_* entry point. */
 enum cunfft_x_status {
   CUNFFT_X_SUCCESS = 0,
@@ -161,6 +171,14 @@ int cunfft_x_set_spread_kernel(cunfft_x_plan *plan, int kind);
 
 /** Spreading kernel in use: CUNFFT_X_SPREAD_SHARED, _REGISTER, _TENSOR or _GLOBAL. */
 int cunfft_x_get_spread_kernel(const cunfft_x_plan *plan, int *kind);
+
+/** Request an interpolation kernel (CUNFFT_X_INTERP_AUTO, _SHARED or _TENSOR);
+ *  TENSOR on a plan it does not cover returns CUNFFT_X_UNSUPPORTED.  The request
+ *  holds across later tilings (a tiling TENSOR does not cover runs SHARED). */
+int cunfft_x_set_interp_kernel(cunfft_x_plan *plan, int kind);
+
+/** Interpolation kernel in use: CUNFFT_X_INTERP_SHARED, _TENSOR or _GLOBAL. */
+int cunfft_x_get_interp_kernel(const cunfft_x_plan *plan, int *kind);
 
 /** Per-stage device times of the last forward/adjoint call, in seconds
  *  (binning, roll-off, FFT, gridding).  Blocks until the plan stream is idle. */
