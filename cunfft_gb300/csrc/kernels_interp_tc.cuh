@@ -51,9 +51,9 @@ __host__ __device__ constexpr bool interp_tc_ok(int d, int W, int T0, int64_t n2
 struct ItLayout {
   uint32_t a_bytes;    // one A part: 16 row groups
   uint32_t b_bytes;    // one B part: N / 8 row groups
-  uint32_t a_off;      // A hi, A lo
+  uint32_t a_off;      // 2 buffers x (A hi, A lo)
   uint32_t b_off;      // 2 buffers x (B hi, B lo)
-  uint32_t bar_off;    // afull, bfull[2], bempty[2], tfull[2], tempty[2]; tensor-memory base
+  uint32_t bar_off;    // afull[2], bfull[2], bempty[2], tfull[2], tempty[2]; tensor-memory base
   uint32_t total;
 };
 
@@ -62,10 +62,55 @@ __host__ __device__ inline ItLayout it_layout(int W) {
   L.a_bytes = 16u * kItSBOA;
   L.b_bytes = (uint32_t)(it_n(W) / 8) * kItSBOB;
   L.a_off = 0;
-  L.b_off = 2u * L.a_bytes;
+  L.b_off = 4u * L.a_bytes;
   L.bar_off = (L.b_off + 4u * L.b_bytes + 15u) & ~15u;
   L.total = L.bar_off + 96u;
   return L;
+}
+
+// Position in this CTA's batch sequence: items c, c + G, ... (CTA c of G; items are
+// never empty) and the batch of up to 128 nodes within the item; the following
+// item's descriptor is loaded one item ahead.
+struct ItCursor {
+  int it, b;
+  int4 item, next;
+};
+__device__ __forceinline__ void it_cursor_init(ItCursor& c, const Bins& bins, int num_items) {
+  const int G = (int)gridDim.x;
+  c.it = (int)blockIdx.x;
+  c.b = 0;
+  c.item = c.it < num_items ? bins.items[c.it] : make_int4(0, 0, 0, 0);
+  c.next = c.it + G < num_items ? bins.items[c.it + G] : make_int4(0, 0, 0, 0);
+}
+__device__ __forceinline__ void it_cursor_step(ItCursor& c, const Bins& bins, int num_items) {
+  const int G = (int)gridDim.x;
+  if (c.it >= num_items) return;
+  if (c.item.y + (++c.b) * kItNodes < c.item.z) return;
+  c.it += G;
+  c.b = 0;
+  c.item = c.next;
+  c.next = c.it + G < num_items ? bins.items[c.it + G] : make_int4(0, 0, 0, 0);
+}
+
+// One node's record, loaded from the bins into registers ahead of use.
+struct ItRec {
+  uint32_t off;  // packed window start (all ones: no node)
+  float fr0, fr1, fr2;
+  int idx;       // output index, -1: no node
+};
+__device__ __forceinline__ ItRec it_load_rec(const ItCursor& c, int num_items, int slot, const Bins& bins) {
+  ItRec r{0xFFFFFFFFu, 0.f, 0.f, 0.f, -1};
+  if (c.it >= num_items) return r;
+  const int j = c.item.y + c.b * kItNodes + slot;
+  if (j < c.item.z) {
+    const float* sfrac = reinterpret_cast<const float*>(bins.sfrac);
+    r.off = (uint32_t)bins.soff[j];
+    r.fr0 = sfrac[(int64_t)j * 3];
+    r.fr1 = sfrac[(int64_t)j * 3 + 1];
+    r.fr2 = sfrac[(int64_t)j * 3 + 2];
+    r.idx = bins.sidx[j];
+  }
+  return r;
 }
 
 template <int W>
@@ -75,17 +120,18 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const float2* __res
   constexpr int E0MAX = kItMaxT0 + W - 1;
   constexpr int MAXCH = (E0MAX + CH - 1) / CH;
   constexpr int PPAD = it_pairs_pad(W);
+  constexpr int BIT = (PPAD + kItBuilders * 8 - 1) / (kItBuilders * 8);  // pair blocks per builder warp
   constexpr int SH = off_bits(3);
   constexpr uint32_t MASK = (1u << SH) - 1u;
   static_assert(NCOL <= 256 && N <= 256 && 2 * N <= 512, "two chunk accumulators must fit tensor memory");
   static_assert(fixed_t_last(3, W) + W - 1 <= kItK, "innermost padded extent must fit K");
   extern __shared__ __align__(16) unsigned char smem[];
   const ItLayout L = it_layout(W);
-  uint64_t* afull = reinterpret_cast<uint64_t*>(smem + L.bar_off);  // A of the batch built
-  uint64_t* bfull = afull + 1;                                       // [2] tile chunk built
-  uint64_t* bempty = afull + 3;                                      // [2] MMAs of the chunk complete
-  uint64_t* tfull = afull + 5;                                       // [2] accumulator complete
-  uint64_t* tempty = afull + 7;                                      // [2] accumulator read out
+  uint64_t* afull = reinterpret_cast<uint64_t*>(smem + L.bar_off);  // [2] A of the batch built
+  uint64_t* bfull = afull + 2;                                       // [2] tile chunk built
+  uint64_t* bempty = afull + 4;                                      // [2] MMAs of the chunk complete
+  uint64_t* tfull = afull + 6;                                       // [2] accumulator complete
+  uint64_t* tempty = afull + 8;                                      // [2] accumulator read out
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + L.bar_off + 80);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int E0 = tl.E[0];
@@ -94,8 +140,8 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const float2* __res
   const int G = (int)gridDim.x;
 
   if (tid == 0) {
-    tc::mbar_init(afull, 128);
     for (int i = 0; i < 2; ++i) {
+      tc::mbar_init(&afull[i], 128);
       tc::mbar_init(&bfull[i], kItBuilders * 32);
       tc::mbar_init(&bempty[i], 1);
       tc::mbar_init(&tfull[i], 1);
@@ -133,35 +179,47 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const float2* __res
           unsigned char* bh = smem + L.b_off + buf * 2u * L.b_bytes;
           unsigned char* bl = bh + L.b_bytes;
           const int ps = c * CH, np = min(CH, E0 - ps);
-          // item (pair, quad): pair = (plane, row) of the chunk, quad = 4 consecutive p2
-          for (int pb = warp * 8; pb < PPAD; pb += kItBuilders * 8) {
-            const int pair = pb + pl8;
+          // item (pair, quad): pair = (plane, row) of the chunk, quad = 4 consecutive p2;
+          // all of this thread's loads go out before the first conversion
+          float4 v[BIT][2][2];
+#pragma unroll
+          for (int i = 0; i < BIT; ++i) {
+            const int pair = warp * 8 + i * kItBuilders * 8 + pl8;
             const int pl = pair / E1, p1 = pair - pl * E1;
             const bool on = pl < np;
             int64_t rowg = 0;
             if (on) rowg = (wrap_pow2(o.a[0] + ps + pl, n0) * n1 + wrap_pow2(o.a[1] + p1, n1)) * n2;
 #pragma unroll
             for (int qh = 0; qh < 2; ++qh) {
-              const int q = qh * 4 + qq;  // p2 = 4q .. 4q + 3 (a quad never straddles the wrap: n2 % 4 == 0)
-              float4 v0 = make_float4(0.f, 0.f, 0.f, 0.f), v1 = v0;
+              const int qd = qh * 4 + qq;  // p2 = 4 qd .. 4 qd + 3 (never straddles the wrap: n2 % 4 == 0)
+              v[i][qh][0] = v[i][qh][1] = make_float4(0.f, 0.f, 0.f, 0.f);
               if (on) {
-                const float4* src = reinterpret_cast<const float4*>(gi + rowg + wrap_pow2(o.a[2] + 4 * q, n2));
-                v0 = src[0];
-                v1 = src[1];
+                const float4* src = reinterpret_cast<const float4*>(gi + rowg + wrap_pow2(o.a[2] + 4 * qd, n2));
+                v[i][qh][0] = src[0];
+                v[i][qh][1] = src[1];
               }
-              const float4 re = make_float4(v0.x, v0.z, v1.x, v1.z), im = make_float4(v0.y, v0.w, v1.y, v1.w);
-              float4 h, l;
-              const int nr = 2 * pair;
-              const uint32_t ore = (uint32_t)(nr >> 3) * kItSBOB + (uint32_t)q * kItLBO + (uint32_t)(nr & 7) * 16u;
-              const uint32_t oim = ore + 16u;  // row 2 pair + 1: same group (nr even)
-              h.x = tc::tf32_round(re.x); h.y = tc::tf32_round(re.y); h.z = tc::tf32_round(re.z); h.w = tc::tf32_round(re.w);
-              l = make_float4(re.x - h.x, re.y - h.y, re.z - h.z, re.w - h.w);
-              *reinterpret_cast<float4*>(bh + ore) = h;
-              *reinterpret_cast<float4*>(bl + ore) = l;
-              h.x = tc::tf32_round(im.x); h.y = tc::tf32_round(im.y); h.z = tc::tf32_round(im.z); h.w = tc::tf32_round(im.w);
-              l = make_float4(im.x - h.x, im.y - h.y, im.z - h.z, im.w - h.w);
-              *reinterpret_cast<float4*>(bh + oim) = h;
-              *reinterpret_cast<float4*>(bl + oim) = l;
+            }
+          }
+#pragma unroll
+          for (int i = 0; i < BIT; ++i) {
+            const int pair = warp * 8 + i * kItBuilders * 8 + pl8;
+            if (pair < PPAD) {
+#pragma unroll
+              for (int qh = 0; qh < 2; ++qh) {
+                const int qd = qh * 4 + qq;
+                const float4 v0 = v[i][qh][0], v1 = v[i][qh][1];
+                const float4 re = make_float4(v0.x, v0.z, v1.x, v1.z), im = make_float4(v0.y, v0.w, v1.y, v1.w);
+                float4 h, l;
+                const int nr = 2 * pair;
+                const uint32_t ore = (uint32_t)(nr >> 3) * kItSBOB + (uint32_t)qd * kItLBO + (uint32_t)(nr & 7) * 16u;
+                const uint32_t oim = ore + 16u;  // row 2 pair + 1: same group (nr even)
+                tc_split4(re, h, l);
+                *reinterpret_cast<float4*>(bh + ore) = h;
+                *reinterpret_cast<float4*>(bl + ore) = l;
+                tc_split4(im, h, l);
+                *reinterpret_cast<float4*>(bh + oim) = h;
+                *reinterpret_cast<float4*>(bl + oim) = l;
+              }
             }
           }
           tc::fence_proxy_async_smem();
@@ -173,6 +231,7 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const float2* __res
     // ======================= MMA issuer: lane 0 =======================
     if (lane == 0) {
       const uint32_t sa = tc::smem_u32(smem + L.a_off), sb = tc::smem_u32(smem + L.b_off);
+      const uint64_t d_abuf = (uint64_t)((2u * L.a_bytes) >> 4);  // A buffer 1 = buffer 0 + d_abuf
       const uint64_t d_ah = tc::smem_desc(sa, kItLBO, kItSBOA);
       const uint64_t d_al = tc::smem_desc(sa + L.a_bytes, kItLBO, kItSBOA);
       const uint64_t d_bh = tc::smem_desc(sb, kItLBO, kItSBOB);
@@ -184,7 +243,9 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const float2* __res
         const int4 item = bins.items[it];
         const int nbatch = (item.z - item.y + kItNodes - 1) / kItNodes;
         for (int bt = 0; bt < nbatch; ++bt, ++gbt) {
-          healthy &= tc::mbar_wait_bounded(afull, gbt & 1u, kItPolls);
+          const uint32_t ab = gbt & 1u;
+          healthy &= tc::mbar_wait_bounded(&afull[ab], (gbt >> 1) & 1u, kItPolls);
+          const uint64_t ao = ab ? d_abuf : 0ull;
           for (int c = 0; c < nch; ++c, ++gc) {
             const uint32_t buf = gc & 1u;
             healthy &= tc::mbar_wait_bounded(&bfull[buf], (gc >> 1) & 1u, kItPolls);
@@ -195,9 +256,9 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const float2* __res
 #pragma unroll
             for (int ks = 0; ks < kItK / 8; ++ks) {
               const uint64_t ko = (uint64_t)((ks * 2 * kItLBO) >> 4);
-              tc::mma_tf32(d, d_ah + ko, d_bh + bo + ko, idesc, ks > 0 ? 1u : 0u);
-              tc::mma_tf32(d, d_ah + ko, d_bl + bo + ko, idesc, 1u);
-              tc::mma_tf32(d, d_al + ko, d_bh + bo + ko, idesc, 1u);
+              tc::mma_tf32(d, d_ah + ao + ko, d_bh + bo + ko, idesc, ks > 0 ? 1u : 0u);
+              tc::mma_tf32(d, d_ah + ao + ko, d_bl + bo + ko, idesc, 1u);
+              tc::mma_tf32(d, d_al + ao + ko, d_bh + bo + ko, idesc, 1u);
             }
             tc::mma_commit(&bempty[buf]);
             tc::mma_commit(&tfull[buf]);
@@ -211,89 +272,91 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const float2* __res
     __syncwarp();
   } else {
     // ======================= node warps: A, then the w0 (x) w1 reduction =======================
+    // Records are loaded two batches ahead; A of batch gbt + 1 is built at the start
+    // of batch gbt (its buffer's previous batch, gbt - 1, is complete: this thread
+    // waited for all of its accumulators), so the MMAs never wait for A.
     const int q = warp & 3;             // tensor-memory lane quarter
     const int slot = 32 * q + lane;     // node slot in the batch = TMEM lane = A row
-    const float* sfrac = reinterpret_cast<const float*>(bins.sfrac);
     const float norm = (float)geo.norm;
     const float mf = (float)geo.m;
     const float cb0 = geo.cbf[0], cb1 = geo.cbf[1], cb2 = geo.cbf[2];
-    unsigned char* ah = smem + L.a_off;
-    unsigned char* al = ah + L.a_bytes;
+    auto build_a = [&](const ItRec& r, uint32_t ab) {
+      unsigned char* ah = smem + L.a_off + ab * 2u * L.a_bytes;
+      unsigned char* al = ah + L.a_bytes;
+      const int o2 = (int)(r.off >> (2 * SH));
+#pragma unroll
+      for (int k4 = 0; k4 < kItK / 4; ++k4) {
+        float4 v;
+        v.x = tc_tap(r.fr2, mf, 4 * k4 + 0 - o2, W, cb2);
+        v.y = tc_tap(r.fr2, mf, 4 * k4 + 1 - o2, W, cb2);
+        v.z = tc_tap(r.fr2, mf, 4 * k4 + 2 - o2, W, cb2);
+        v.w = tc_tap(r.fr2, mf, 4 * k4 + 3 - o2, W, cb2);
+        float4 h, l;
+        tc_split4(v, h, l);
+        const uint32_t oa = (uint32_t)(slot >> 3) * kItSBOA + (uint32_t)k4 * kItLBO + (uint32_t)(slot & 7) * 16u;
+        *reinterpret_cast<float4*>(ah + oa) = h;
+        *reinterpret_cast<float4*>(al + oa) = l;
+      }
+      tc::fence_proxy_async_smem();
+      tc::mbar_arrive(&afull[ab]);
+    };
+    ItCursor c0, c1, c2;  // batches gbt, gbt + 1, gbt + 2
+    it_cursor_init(c0, bins, num_items);
+    c1 = c0;
+    it_cursor_step(c1, bins, num_items);
+    c2 = c1;
+    it_cursor_step(c2, bins, num_items);
+    ItRec rc = it_load_rec(c0, num_items, slot, bins), rn = it_load_rec(c1, num_items, slot, bins);
+    if (c0.it < num_items) build_a(rc, 0u);
     uint32_t gc = 0, gbt = 0;
-    for (int it = blockIdx.x; it < num_items; it += G) {
-      const int4 item = bins.items[it];
-      const int nbatch = (item.z - item.y + kItNodes - 1) / kItNodes;
-      for (int bt = 0; bt < nbatch; ++bt, ++gbt) {
-        const int j = item.y + bt * kItNodes + slot;
-        const bool valid = j < item.z;
-        uint32_t off = 0xFFFFFFFFu;  // no window: every tap zero
-        float fr0 = 0.f, fr1 = 0.f, fr2 = 0.f;
-        int idx = 0;
-        if (valid) {
-          off = (uint32_t)bins.soff[j];
-          fr0 = sfrac[(int64_t)j * 3];
-          fr1 = sfrac[(int64_t)j * 3 + 1];
-          fr2 = sfrac[(int64_t)j * 3 + 2];
-          idx = bins.sidx[j];
-        }
-        const int o0 = (int)(off & MASK), o1 = (int)((off >> SH) & MASK), o2 = (int)(off >> (2 * SH));
-        // A row `slot`: w2 over the 32 columns (the MMAs of the previous batch are complete:
-        // this thread waited for its last accumulator)
+    for (; c0.it < num_items; ++gbt) {
+      if (c1.it < num_items) build_a(rn, (gbt + 1u) & 1u);
+      const ItRec rnn = it_load_rec(c2, num_items, slot, bins);
+      const int o0 = (int)(rc.off & MASK), o1 = (int)((rc.off >> SH) & MASK);
+      // expanded w0 (planes) and w1 (rows) of this node
+      float w0x[E0MAX], w1x[E1];
 #pragma unroll
-        for (int k4 = 0; k4 < kItK / 4; ++k4) {
-          float4 v;
-          v.x = tc_tap(fr2, mf, 4 * k4 + 0 - o2, W, cb2);
-          v.y = tc_tap(fr2, mf, 4 * k4 + 1 - o2, W, cb2);
-          v.z = tc_tap(fr2, mf, 4 * k4 + 2 - o2, W, cb2);
-          v.w = tc_tap(fr2, mf, 4 * k4 + 3 - o2, W, cb2);
-          float4 h, l;
-          tc_split4(v, h, l);
-          const uint32_t oa = (uint32_t)(slot >> 3) * kItSBOA + (uint32_t)k4 * kItLBO + (uint32_t)(slot & 7) * 16u;
-          *reinterpret_cast<float4*>(ah + oa) = h;
-          *reinterpret_cast<float4*>(al + oa) = l;
-        }
-        tc::fence_proxy_async_smem();
-        tc::mbar_arrive(afull);
-        // expanded w0 (planes) and w1 (rows) of this node
-        float w0x[E0MAX], w1x[E1];
+      for (int p = 0; p < E0MAX; ++p) w0x[p] = tc_tap(rc.fr0, mf, p - o0, W, cb0);
 #pragma unroll
-        for (int p = 0; p < E0MAX; ++p) w0x[p] = tc_tap(fr0, mf, p - o0, W, cb0);
+      for (int p = 0; p < E1; ++p) w1x[p] = tc_tap(rc.fr1, mf, p - o1, W, cb1);
+      float accx = 0.f, accy = 0.f;
 #pragma unroll
-        for (int p = 0; p < E1; ++p) w1x[p] = tc_tap(fr1, mf, p - o1, W, cb1);
-        float accx = 0.f, accy = 0.f;
+      for (int c = 0; c < MAXCH; ++c) {
+        if (c < nch) {
+          const uint32_t buf = gc & 1u;
+          healthy &= tc::mbar_wait_bounded(&tfull[buf], (gc >> 1) & 1u, kItPolls);
+          __syncwarp();
+          tc::fence_after_sync();
+          const uint32_t t0 = tmem + ((uint32_t)(32 * q) << 16) + buf * 256u;
 #pragma unroll
-        for (int c = 0; c < MAXCH; ++c) {
-          if (c < nch) {
-            const uint32_t buf = gc & 1u;
-            healthy &= tc::mbar_wait_bounded(&tfull[buf], (gc >> 1) & 1u, kItPolls);
-            __syncwarp();
-            tc::fence_after_sync();
-            const uint32_t t0 = tmem + ((uint32_t)(32 * q) << 16) + buf * 256u;
+          for (int gi = 0; gi < N / 16; ++gi) {
+            float v[16];
+            tc::tmem_ld16(t0 + (uint32_t)(gi * 16), v);
+            tc::tmem_ld_wait();
 #pragma unroll
-            for (int gi = 0; gi < N / 16; ++gi) {
-              float v[16];
-              tc::tmem_ld16(t0 + (uint32_t)(gi * 16), v);
-              tc::tmem_ld_wait();
-#pragma unroll
-              for (int u = 0; u < 16; u += 2) {
-                const int col = gi * 16 + u;  // (re, im) of (plane pl, row p1)
-                if (col < NCOL) {
-                  const int pl = col / (2 * E1), p1 = (col % (2 * E1)) / 2;
-                  if (c * CH + pl < E0MAX) {
-                    const float w = w0x[c * CH + pl] * w1x[p1];
-                    accx = fmaf(w, v[u], accx);
-                    accy = fmaf(w, v[u + 1], accy);
-                  }
+            for (int u = 0; u < 16; u += 2) {
+              const int col = gi * 16 + u;  // (re, im) of (plane pl, row p1)
+              if (col < NCOL) {
+                const int pl = col / (2 * E1), p1 = (col % (2 * E1)) / 2;
+                if (c * CH + pl < E0MAX) {
+                  const float w = w0x[c * CH + pl] * w1x[p1];
+                  accx = fmaf(w, v[u], accx);
+                  accy = fmaf(w, v[u + 1], accy);
                 }
               }
             }
-            tc::fence_before_sync();
-            tc::mbar_arrive(&tempty[buf]);
-            ++gc;
           }
+          tc::fence_before_sync();
+          tc::mbar_arrive(&tempty[buf]);
+          ++gc;
         }
-        if (valid) f[idx] = make_float2(accx * norm, accy * norm);
       }
+      if (rc.idx >= 0) f[rc.idx] = make_float2(accx * norm, accy * norm);
+      rc = rn;
+      rn = rnn;
+      c0 = c1;
+      c1 = c2;
+      it_cursor_step(c2, bins, num_items);
     }
   }
   tc::fence_before_sync();
