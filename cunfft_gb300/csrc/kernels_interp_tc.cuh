@@ -141,11 +141,11 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const float2* __res
 
   if (tid == 0) {
     for (int i = 0; i < 2; ++i) {
-      tc::mbar_init(&afull[i], 128);
-      tc::mbar_init(&bfull[i], kItBuilders * 32);
+      tc::mbar_init(&afull[i], 4);             // one arrival per node warp
+      tc::mbar_init(&bfull[i], kItBuilders);   // one arrival per builder warp
       tc::mbar_init(&bempty[i], 1);
       tc::mbar_init(&tfull[i], 1);
-      tc::mbar_init(&tempty[i], 128);
+      tc::mbar_init(&tempty[i], 4);            // one arrival per node warp
     }
     tc::mbar_fence_init();
   }
@@ -175,7 +175,7 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const float2* __res
       for (int bt = 0; bt < nbatch; ++bt) {
         for (int c = 0; c < nch; ++c, ++gc) {
           const uint32_t buf = gc & 1u;
-          if (gc >= 2) healthy &= tc::mbar_wait_bounded(&bempty[buf], ((gc >> 1) - 1u) & 1u, kItPolls);
+          if (gc >= 2) healthy &= tc::mbar_wait_warp(&bempty[buf], ((gc >> 1) - 1u) & 1u, kItPolls);
           unsigned char* bh = smem + L.b_off + buf * 2u * L.b_bytes;
           unsigned char* bl = bh + L.b_bytes;
           const int ps = c * CH, np = min(CH, E0 - ps);
@@ -223,7 +223,7 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const float2* __res
             }
           }
           tc::fence_proxy_async_smem();
-          tc::mbar_arrive(&bfull[buf]);
+          tc::mbar_arrive_warp(&bfull[buf]);
         }
       }
     }
@@ -298,7 +298,7 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const float2* __res
         *reinterpret_cast<float4*>(al + oa) = l;
       }
       tc::fence_proxy_async_smem();
-      tc::mbar_arrive(&afull[ab]);
+      tc::mbar_arrive_warp(&afull[ab]);
     };
     ItCursor c0, c1, c2;  // batches gbt, gbt + 1, gbt + 2
     it_cursor_init(c0, bins, num_items);
@@ -324,8 +324,7 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const float2* __res
       for (int c = 0; c < MAXCH; ++c) {
         if (c < nch) {
           const uint32_t buf = gc & 1u;
-          healthy &= tc::mbar_wait_bounded(&tfull[buf], (gc >> 1) & 1u, kItPolls);
-          __syncwarp();
+          healthy &= tc::mbar_wait_warp(&tfull[buf], (gc >> 1) & 1u, kItPolls);
           tc::fence_after_sync();
           const uint32_t t0 = tmem + ((uint32_t)(32 * q) << 16) + buf * 256u;
 #pragma unroll
@@ -347,7 +346,7 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const float2* __res
             }
           }
           tc::fence_before_sync();
-          tc::mbar_arrive(&tempty[buf]);
+          tc::mbar_arrive_warp(&tempty[buf]);
           ++gc;
         }
       }

@@ -71,6 +71,23 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(bar)) : "memory");
 }
 
+// Warp-wide hand-offs on an mbarrier whose count is in warps: one arrival or one
+// poller per (converged) warp instead of 32 same-address operations, which the
+// shared-memory pipe would serialise.  __syncwarp orders every lane's earlier
+// shared-memory writes before lane 0's release, and lane 0's acquire before every
+// lane's later accesses.
+__device__ __forceinline__ void mbar_arrive_warp(uint64_t* bar) {
+  __syncwarp();
+  if ((threadIdx.x & 31) == 0) mbar_arrive(bar);
+}
+__device__ __forceinline__ bool mbar_wait_warp(uint64_t* bar, uint32_t parity, uint32_t max_polls) {
+  uint32_t ok = 1;
+  if ((threadIdx.x & 31) == 0) ok = mbar_wait_bounded(bar, parity, max_polls) ? 1u : 0u;
+  ok = __shfl_sync(0xffffffffu, ok, 0);
+  __syncwarp();
+  return ok != 0;
+}
+
 // named barrier among `count` threads (a multiple of 32) of the CTA
 __device__ __forceinline__ void named_sync(uint32_t id, uint32_t count) {
   asm volatile("bar.sync %0, %1;\n" ::"r"(id), "r"(count) : "memory");
