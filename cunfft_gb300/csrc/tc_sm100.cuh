@@ -166,10 +166,13 @@ __device__ __forceinline__ void tc_split4(float4 v, float4& hi, float4& lo) {
 }
 
 // Gaussian tap exp(-(fr + m - l)^2 / b) = exp2(-(fr + m - l)^2 cb), the FP32 tap of
-// WeightMath<float>::taps (cb = log2(e) / b), zero outside the window 0 <= l < W
+// WeightMath<float>::taps (cb = log2(e) / b), zero outside the window 0 <= l < W.
+// The exponential is evaluated for every l and then selected: lanes hold different
+// windows, and a branch around it would diverge on every tap.
 __device__ __forceinline__ float tc_tap(float fr, float mf, int l, int W, float cb) {
   const float y = fr + (mf - (float)l);
-  return (unsigned)l < (unsigned)W ? exp2f(-(y * y) * cb) : 0.f;
+  const float e = exp2f(-(y * y) * cb);
+  return (unsigned)l < (unsigned)W ? e : 0.f;
 }
 
 }  // namespace cg
