@@ -40,7 +40,7 @@ __global__ void k_bin_count(const double* __restrict__ x, int64_t M, Geom geo, T
       int64_t u; double c;
       reduce_coord(x[j * d + t], geo.n[t], geo.m, u, c);
       int64_t s = wrap_pow2(u, geo.n[t]);
-      tile = tile * tl.nb[t] + s / tl.T[t];
+      tile = tile * tl.nb[t] + (s >> (__ffs(tl.T[t]) - 1));  // T_t is a power of two
     }
     tile += (int64_t)inst * tl.tiles_per_inst;
     int rank = atomicAdd(&count[tile], 1);
@@ -61,7 +61,7 @@ __global__ void k_bin_scatter(const double* __restrict__ x, int64_t M, Geom geo,
       int64_t u; double c;
       reduce_coord(x[j * d + t], geo.n[t], geo.m, u, c);
       int64_t s = wrap_pow2(u, geo.n[t]);
-      uint32_t o = (uint32_t)(s % tl.T[t]);
+      uint32_t o = (uint32_t)(s & (tl.T[t] - 1));  // T_t is a power of two
       packed |= o << (off_bits_host(d) * t);
       sfrac[pos * d + t] = (T)(c - (double)geo.m);
     }
@@ -71,42 +71,63 @@ __global__ void k_bin_scatter(const double* __restrict__ x, int64_t M, Geom geo,
 }
 
 // Single-CTA exclusive scan of the per-tile counts and of the per-tile work-item
-// counts ceil(count / chunk).  Each thread scans a contiguous segment.
+// counts ceil(count / chunk).  Each thread scans a contiguous segment (loads
+// unrolled so several are in flight); the segment totals are scanned with warp
+// shuffles and one shared-memory pass over the 32 warp totals.
+__device__ __forceinline__ void warp_incl_scan2(int64_t& a, int64_t& b) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int64_t x = __shfl_up_sync(0xffffffffu, a, o), y = __shfl_up_sync(0xffffffffu, b, o);
+    if (lane >= o) {
+      a += x;
+      b += y;
+    }
+  }
+}
+
 __global__ void __launch_bounds__(1024) k_scan_tiles(const int32_t* __restrict__ count, int64_t ntiles, int chunk,
                                                      int32_t* __restrict__ tile_off, int32_t* __restrict__ item_off,
                                                      int32_t* __restrict__ num_items) {
-  __shared__ int64_t sc[1024], si[1024];
-  const int tid = threadIdx.x, nt = blockDim.x;
+  __shared__ int64_t wc[32], wi[32];
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
   const int64_t seg = (ntiles + nt - 1) / nt;
   const int64_t lo = min(ntiles, tid * seg), hi = min(ntiles, lo + seg);
   int64_t c = 0, it = 0;
+#pragma unroll 8
   for (int64_t i = lo; i < hi; ++i) {
-    int32_t v = count[i];
+    const int32_t v = count[i];
     c += v;
     it += (v + chunk - 1) / chunk;
   }
-  sc[tid] = c;
-  si[tid] = it;
-  __syncthreads();
-  for (int off = 1; off < nt; off <<= 1) {
-    int64_t a = tid >= off ? sc[tid - off] : 0, b = tid >= off ? si[tid - off] : 0;
-    __syncthreads();
-    sc[tid] += a;
-    si[tid] += b;
-    __syncthreads();
+  int64_t ic = c, ii = it;  // inclusive scan over the block
+  warp_incl_scan2(ic, ii);
+  if (lane == 31) {
+    wc[warp] = ic;
+    wi[warp] = ii;
   }
-  int64_t rc = sc[tid] - c, ri = si[tid] - it;
+  __syncthreads();
+  if (warp == 0) {
+    int64_t a = lane < nt / 32 ? wc[lane] : 0, b = lane < nt / 32 ? wi[lane] : 0;
+    warp_incl_scan2(a, b);
+    wc[lane] = a;
+    wi[lane] = b;
+  }
+  __syncthreads();
+  const int64_t base_c = warp > 0 ? wc[warp - 1] : 0, base_i = warp > 0 ? wi[warp - 1] : 0;
+  int64_t rc = base_c + ic - c, ri = base_i + ii - it;
+#pragma unroll 8
   for (int64_t i = lo; i < hi; ++i) {
-    int32_t v = count[i];
+    const int32_t v = count[i];
     tile_off[i] = (int32_t)rc;
     item_off[i] = (int32_t)ri;
     rc += v;
     ri += (v + chunk - 1) / chunk;
   }
   if (tid == nt - 1) {
-    tile_off[ntiles] = (int32_t)sc[tid];
-    item_off[ntiles] = (int32_t)si[tid];
-    *num_items = (int32_t)si[tid];
+    tile_off[ntiles] = (int32_t)(base_c + ic);
+    item_off[ntiles] = (int32_t)(base_i + ii);
+    *num_items = (int32_t)(base_i + ii);
   }
 }
 

@@ -12,77 +12,121 @@
 
 namespace cg {
 
-template <typename T>
+// log2 of the power-of-two grid sizes, computed on the host
+struct RocShifts {
+  int lg_n[kMaxDim];
+  int lg_ntot;
+};
+
+// Frequency slot c = k + floor(N/2) of grid index i along a dimension (k = i or i - n),
+// or -1 when i lies in the zero padding.
+__device__ __forceinline__ int64_t roc_slot(int64_t i, int64_t N, int64_t n) {
+  const int64_t half = N / 2;
+  if (i < N - half) return i + half;
+  if (i >= n - half) return i - n + half;
+  return -1;
+}
+
+// EPT consecutive grid points per thread (2 when the last grid size is even, so a
+// pair never leaves its row; 1 otherwise); integer decoding by shifts only, and the
+// FP64 factor product, in the order dimension 0, 1, ..., only for points inside I_N
+// (one in 2^d of the grid).
+template <typename T, int EPT>
 __global__ void k_roc_forward(const typename Cx<T>::t* __restrict__ fhat, typename Cx<T>::t* __restrict__ g,
-                              Geom geo, const double* __restrict__ tab) {
+                              Geom geo, const double* __restrict__ tab, RocShifts sh) {
   using C = typename Cx<T>::t;
   const int d = geo.d;
-  const int64_t total = geo.ntot * geo.batch;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-    int64_t inst = e / geo.ntot, gi = e - inst * geo.ntot;
-    int64_t ci = 0;
+  const int64_t total2 = geo.ntot * geo.batch / EPT;
+  const int64_t n_last = geo.n[d - 1], N_last = geo.N[d - 1];
+  for (int64_t e2 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e2 < total2;
+       e2 += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e = EPT * e2;
+    const int64_t inst = e >> sh.lg_ntot, gi = e & (geo.ntot - 1);
+    const int64_t i_last = gi & (n_last - 1);
+    int64_t rest = gi >> sh.lg_n[d - 1];
+    // leading dimensions 0 .. d-2
+    int64_t lead_idx[kMaxDim];
+    for (int t = d - 2; t >= 0; --t) {
+      lead_idx[t] = rest & (geo.n[t] - 1);
+      rest >>= sh.lg_n[t];
+    }
+    bool lead_in = true;
+    int64_t ci = 0, tab_base = 0;
     double fac = 1.0;
-    bool inside = true;
-    int64_t rem = gi, tab_base = 0;
-    int64_t idx[kMaxDim];
-    for (int t = d - 1; t >= 0; --t) {
-      idx[t] = rem & (geo.n[t] - 1);
-      rem >>= __ffsll(geo.n[t]) - 1;
+    for (int t = 0; t < d - 1 && lead_in; ++t) {
+      const int64_t c = roc_slot(lead_idx[t], geo.N[t], geo.n[t]);
+      if (c < 0) {
+        lead_in = false;
+      } else {
+        ci = ci * geo.N[t] + c;
+        fac *= tab[tab_base + c];
+        tab_base += geo.N[t];
+      }
     }
-    for (int t = 0; t < d; ++t) {
-      const int64_t Nt = geo.N[t], half = Nt / 2, i = idx[t];
-      int64_t k;
-      if (i < Nt - half) k = i;
-      else if (i >= geo.n[t] - half) k = i - geo.n[t];
-      else { inside = false; break; }
-      const int64_t c = k + half;
-      ci = ci * Nt + c;
-      fac *= tab[tab_base + c];
-      tab_base += Nt;
+    C out[EPT];
+#pragma unroll
+    for (int u = 0; u < EPT; ++u) {
+      out[u].x = (T)0;
+      out[u].y = (T)0;
+      const int64_t c = lead_in ? roc_slot(i_last + u, N_last, n_last) : -1;
+      if (c >= 0) {
+        const C a = fhat[inst * geo.Ntot + ci * N_last + c];
+        const T s = (T)(fac * tab[tab_base + c]);
+        out[u].x = a.x * s;
+        out[u].y = a.y * s;
+      }
     }
-    C out;
-    if (inside) {
-      C a = fhat[inst * geo.Ntot + ci];
-      T s = (T)fac;
-      out.x = a.x * s;
-      out.y = a.y * s;
-    } else {
-      out.x = (T)0;
-      out.y = (T)0;
-    }
-    g[e] = out;
+#pragma unroll
+    for (int u = 0; u < EPT; ++u) g[e + u] = out[u];
   }
 }
 
-template <typename T>
+// Coefficient crop; 32-bit index arithmetic when the coefficient count allows it.
+template <typename T, typename I>
 __global__ void k_roc_adjoint(const typename Cx<T>::t* __restrict__ g, typename Cx<T>::t* __restrict__ fhat,
                               Geom geo, const double* __restrict__ tab) {
   using C = typename Cx<T>::t;
   const int d = geo.d;
-  const int64_t total = geo.Ntot * geo.batch;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-    int64_t inst = e / geo.Ntot, ci = e - inst * geo.Ntot;
-    int64_t c[kMaxDim];
-    int64_t rem = ci;
+  const I Ntot = (I)geo.Ntot;
+  const I total = Ntot * (I)geo.batch;
+  for (I e = blockIdx.x * (I)blockDim.x + threadIdx.x; e < total; e += (I)gridDim.x * blockDim.x) {
+    const I inst = geo.batch > 1 ? e / Ntot : (I)0, ci = e - inst * Ntot;
+    I c[kMaxDim];
+    I rem = ci;
     for (int t = d - 1; t >= 0; --t) {
-      c[t] = rem % geo.N[t];
-      rem /= geo.N[t];
+      const I Nt = (I)geo.N[t];
+      const I q = rem / Nt;
+      c[t] = rem - q * Nt;
+      rem = q;
     }
     double fac = 1.0;
-    int64_t gi = 0, tab_base = 0;
+    int64_t gidx = 0, tab_base = 0;
     for (int t = 0; t < d; ++t) {
-      const int64_t k = c[t] - geo.N[t] / 2;
-      gi = gi * geo.n[t] + (k & (geo.n[t] - 1));
+      const int64_t k = (int64_t)c[t] - geo.N[t] / 2;
+      gidx = gidx * geo.n[t] + (k & (geo.n[t] - 1));
       fac *= tab[tab_base + c[t]];
       tab_base += geo.N[t];
     }
-    C a = g[inst * geo.ntot + gi];
-    T s = (T)fac;
+    const C a = g[(int64_t)inst * geo.ntot + gidx];
+    const T s = (T)fac;
     C out;
     out.x = a.x * s;
     out.y = a.y * s;
     fhat[e] = out;
   }
+}
+
+static RocShifts roc_shifts(const Geom& geo) {
+  RocShifts sh{};
+  for (int t = 0; t < kMaxDim; ++t) {
+    int l = 0;
+    while (((int64_t)1 << l) < geo.n[t]) ++l;
+    sh.lg_n[t] = l;
+  }
+  int l = 0;
+  while (((int64_t)1 << l) < geo.ntot) ++l;
+  sh.lg_ntot = l;
+  return sh;
 }
 
 static inline int roc_grid(const Plan& p, int64_t work) {
@@ -92,20 +136,34 @@ static inline int roc_grid(const Plan& p, int64_t work) {
 }
 
 cudaError_t launch_roc_forward(const Plan& p, const void* fhat, void* g, cudaStream_t st) {
-  const int64_t work = p.geo.ntot * p.geo.batch;
-  if (p.prec == kF64)
-    k_roc_forward<double><<<roc_grid(p, work), 256, 0, st>>>((const double2*)fhat, (double2*)g, p.geo, p.roc_tab);
-  else
-    k_roc_forward<float><<<roc_grid(p, work), 256, 0, st>>>((const float2*)fhat, (float2*)g, p.geo, p.roc_tab);
+  const bool pairs = (p.geo.n[p.geo.d - 1] & 1) == 0;
+  const int64_t work = p.geo.ntot * p.geo.batch / (pairs ? 2 : 1);
+  const RocShifts sh = roc_shifts(p.geo);
+  const int blocks = roc_grid(p, work);
+  if (p.prec == kF64) {
+    if (pairs) k_roc_forward<double, 2><<<blocks, 256, 0, st>>>((const double2*)fhat, (double2*)g, p.geo, p.roc_tab, sh);
+    else k_roc_forward<double, 1><<<blocks, 256, 0, st>>>((const double2*)fhat, (double2*)g, p.geo, p.roc_tab, sh);
+  } else {
+    if (pairs) k_roc_forward<float, 2><<<blocks, 256, 0, st>>>((const float2*)fhat, (float2*)g, p.geo, p.roc_tab, sh);
+    else k_roc_forward<float, 1><<<blocks, 256, 0, st>>>((const float2*)fhat, (float2*)g, p.geo, p.roc_tab, sh);
+  }
   return cudaGetLastError();
 }
 
 cudaError_t launch_roc_adjoint(const Plan& p, const void* g, void* fhat, cudaStream_t st) {
   const int64_t work = p.geo.Ntot * p.geo.batch;
-  if (p.prec == kF64)
-    k_roc_adjoint<double><<<roc_grid(p, work), 256, 0, st>>>((const double2*)g, (double2*)fhat, p.geo, p.roc_tab);
-  else
-    k_roc_adjoint<float><<<roc_grid(p, work), 256, 0, st>>>((const float2*)g, (float2*)fhat, p.geo, p.roc_tab);
+  const bool small = work < ((int64_t)1 << 31);
+  if (p.prec == kF64) {
+    if (small)
+      k_roc_adjoint<double, uint32_t><<<roc_grid(p, work), 256, 0, st>>>((const double2*)g, (double2*)fhat, p.geo, p.roc_tab);
+    else
+      k_roc_adjoint<double, int64_t><<<roc_grid(p, work), 256, 0, st>>>((const double2*)g, (double2*)fhat, p.geo, p.roc_tab);
+  } else {
+    if (small)
+      k_roc_adjoint<float, uint32_t><<<roc_grid(p, work), 256, 0, st>>>((const float2*)g, (float2*)fhat, p.geo, p.roc_tab);
+    else
+      k_roc_adjoint<float, int64_t><<<roc_grid(p, work), 256, 0, st>>>((const float2*)g, (float2*)fhat, p.geo, p.roc_tab);
+  }
   return cudaGetLastError();
 }
 
