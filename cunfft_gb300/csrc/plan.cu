@@ -398,18 +398,26 @@ static int rebin(Plan* p) {
 int plan_set_nodes(Plan* p, const double* x, const int64_t* M_inst) {
   int64_t M = 0;
   std::vector<int32_t> off((size_t)p->geo.batch + 1, 0);
+  bool same = p->inst_off_current;
   for (int i = 0; i < p->geo.batch; ++i) {
     if (M_inst[i] < 0) return set_status(p, CUNFFT_X_INVALID_ARGUMENT, "M[%d] < 0", i);
     M += M_inst[i];
     if (M >= ((int64_t)1 << 31) - 1) return set_status(p, CUNFFT_X_UNSUPPORTED, "more than 2^31-2 nodes");
     off[i + 1] = (int32_t)M;
-    p->M_inst[i] = M_inst[i];
+    same = same && p->M_inst[i] == M_inst[i];
   }
   if (M > 0 && !x) return set_status(p, CUNFFT_X_INVALID_ARGUMENT, "x is NULL");
-  CG_TRY(check_cuda(p, cudaMemcpyAsync(p->bins.inst_off, off.data(), sizeof(int32_t) * off.size(),
-                                       cudaMemcpyHostToDevice, p->stream), "upload node offsets"));
-  // the host vector must outlive the async copy
-  CG_TRY(check_cuda(p, cudaStreamSynchronize(p->stream), "cudaStreamSynchronize"));
+  // New per-instance counts: upload the offsets (the host vector must outlive the
+  // copy, hence the wait).  Unchanged counts, the usual case of a moving node set,
+  // need neither the copy nor the wait, so the stream keeps running.
+  if (!same) {
+    p->inst_off_current = false;
+    CG_TRY(check_cuda(p, cudaMemcpyAsync(p->bins.inst_off, off.data(), sizeof(int32_t) * off.size(),
+                                         cudaMemcpyHostToDevice, p->stream), "upload node offsets"));
+    CG_TRY(check_cuda(p, cudaStreamSynchronize(p->stream), "cudaStreamSynchronize"));
+    for (int i = 0; i < p->geo.batch; ++i) p->M_inst[i] = M_inst[i];
+    p->inst_off_current = true;
+  }
   p->x = x;
   p->M = M;
   CG_TRY(rebin(p));

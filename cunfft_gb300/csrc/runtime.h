@@ -39,6 +39,7 @@ struct Plan {
   const double* x = nullptr;   // device nodes of the current node set
   int64_t M = 0;
   int64_t* M_inst = nullptr;   // host copy of per-instance node counts
+  bool inst_off_current = false;  // bins.inst_off holds the offsets of M_inst
   bool nodes_set = false;
   int tile_override[kMaxDim] = {0, 0, 0};
   int chunk_override = 0;
