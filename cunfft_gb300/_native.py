@@ -85,7 +85,7 @@ X_SYMBOLS = [
     "cunfft_x_autotune", "cunfft_x_get_tiling", "cunfft_x_stage_times", "cunfft_x_synchronize",
     "cunfft_x_last_message", "cunfft_x_status_string", "cunfft_x_grid", "cunfft_x_version",
     "cunfft_x_spread_noalloc", "cunfft_x_set_spread_kernel", "cunfft_x_get_spread_kernel",
-    "cunfft_x_set_interp_kernel", "cunfft_x_get_interp_kernel",
+    "cunfft_x_set_interp_kernel", "cunfft_x_get_interp_kernel", "cunfft_x_forward_host", "cunfft_x_adjoint_host",
 ]
 UTIL_SYMBOLS = [
     "showTimes", "getGPUMemProps_ToStdout", "showCPUMemUse", "showCoeff_double", "showCoeff_cuComplex",
@@ -134,6 +134,8 @@ def lib():
         "cunfft_x_get_spread_kernel": (ctypes.c_int, [vp, ip]),
         "cunfft_x_set_interp_kernel": (ctypes.c_int, [vp, ctypes.c_int]),
         "cunfft_x_get_interp_kernel": (ctypes.c_int, [vp, ip]),
+        "cunfft_x_forward_host": (ctypes.c_int, [vp, vp, i64p, vp, vp]),
+        "cunfft_x_adjoint_host": (ctypes.c_int, [vp, vp, vp]),
         "cunfft_x_stage_times": (ctypes.c_int, [vp, dp, dp, dp, dp]),
         "cunfft_x_synchronize": (ctypes.c_int, [vp]),
         "cunfft_x_last_message": (ctypes.c_char_p, [vp]),

@@ -44,12 +44,6 @@ int check_cufft(Plan* p, cufftResult r, const char* what) {
                     "%s: cuFFT error %d", what, (int)r);
 }
 
-#define CG_TRY(expr)                          \
-  do {                                        \
-    int _s = (expr);                          \
-    if (_s != CUNFFT_X_SUCCESS) return _s;    \
-  } while (0)
-
 static bool is_pow2(int64_t v) { return v > 0 && (v & (v - 1)) == 0; }
 
 static size_t elem_bytes(const Plan* p) { return p->prec == kF64 ? 16 : 8; }
@@ -330,6 +324,7 @@ int plan_init(Plan* p, int d, const int64_t* N, const int64_t* n, int m, int pre
 void plan_release(Plan* p) {
   if (!p) return;
   if (p->stream) cudaStreamSynchronize(p->stream);
+  plan_host_path_release(p);
   for (int i = 0; i < 2; ++i)
     if (p->gexec[i]) {
       cudaGraphExecDestroy(p->gexec[i]);

@@ -18,6 +18,8 @@ namespace cg {
 
 enum Precision { kF64 = CUNFFT_X_F64, kF32 = CUNFFT_X_F32 };
 
+struct HostPath;  // copy streams and staging of the host-buffer transforms (hostpath.cpp)
+
 struct Plan {
   Geom geo{};
   int prec = kF64;
@@ -58,7 +60,17 @@ struct Plan {
   void* g_out[2] = {nullptr, nullptr};
   uint64_t g_gen[2] = {0, 0};
   uint64_t node_gen = 0;  // bumped by every node binding / tiling change
+  HostPath* hp = nullptr; // created by the first host-buffer transform
 };
+
+inline size_t plan_elem_bytes(const Plan* p) { return p->prec == kF64 ? 16 : 8; }
+
+// return the status of a runtime call when it is not CUNFFT_X_SUCCESS
+#define CG_TRY(expr)                          \
+  do {                                        \
+    int _s = (expr);                          \
+    if (_s != CUNFFT_X_SUCCESS) return _s;    \
+  } while (0)
 
 // status helpers
 int set_status(Plan* p, int code, const char* fmt, ...);
@@ -79,6 +91,11 @@ int plan_spread_only(Plan* p, const void* f, void* g);
 int plan_ndft_forward(Plan* p, const void* fhat, void* f);
 int plan_ndft_adjoint(Plan* p, const void* f, void* fhat, const int64_t* kidx = nullptr, int64_t nsel = 0);
 int plan_node_gradient(Plan* p, const void* fhat, const void* grad_f, double* grad_x);
+// host-buffer transforms with overlapped copies (hostpath.cpp)
+int plan_forward_host(Plan* p, const double* x_host, const int64_t* M_inst, const void* fhat_host, void* f_host);
+int plan_adjoint_host(Plan* p, const void* f_host, void* fhat_host);
+int plan_host_path_sync(Plan* p);
+void plan_host_path_release(Plan* p);
 int plan_choose_tiling(Plan* p, const int* T, int chunk);
 int plan_autotune(Plan* p, int reps);
 int plan_set_spread_kernel(Plan* p, int kind);

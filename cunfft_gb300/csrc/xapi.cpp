@@ -141,6 +141,17 @@ int cunfft_x_get_spread_kernel(const cunfft_x_plan* h, int* kind) {
   return CUNFFT_X_SUCCESS;
 }
 
+int cunfft_x_forward_host(cunfft_x_plan* h, const double* x_host, const int64_t* M, const void* fhat_host,
+                          void* f_host) {
+  if (!h) return CUNFFT_X_INVALID_ARGUMENT;
+  return cg::plan_forward_host(&h->p, x_host, M, fhat_host, f_host);
+}
+
+int cunfft_x_adjoint_host(cunfft_x_plan* h, const void* f_host, void* fhat_host) {
+  if (!h) return CUNFFT_X_INVALID_ARGUMENT;
+  return cg::plan_adjoint_host(&h->p, f_host, fhat_host);
+}
+
 int cunfft_x_set_interp_kernel(cunfft_x_plan* h, int kind) {
   if (!h) return CUNFFT_X_INVALID_ARGUMENT;
   return cg::plan_set_interp_kernel(&h->p, kind);
@@ -180,6 +191,7 @@ int cunfft_x_synchronize(cunfft_x_plan* h) {
   cg::Plan& p = h->p;
   cudaError_t e = cudaStreamSynchronize(p.stream);
   if (e != cudaSuccess) return cg::check_cuda(&p, e, "cudaStreamSynchronize");
+  CG_TRY(cg::plan_host_path_sync(&p));
   // device-side status: a bounded wait in a kernel that gave up (the flag is cleared on read)
   int32_t flag = 0;
   if (p.bins.status) {

@@ -23,6 +23,7 @@ def _ptr(t):
 
 class NFFT:
     def __init__(self, N, n=None, m=6, precision="f64", batch=1, device=None, stream=None):
+        self._host_refs = []  # host tensors in flight in host-buffer transforms
         self._lib = nat.lib()
         self.N = [int(v) for v in N]
         self.d = len(self.N)
@@ -111,6 +112,44 @@ class NFFT:
         fh = out if out is not None else torch.empty(self._coef_shape(), dtype=self.cdtype, device=self.device)
         nat.check(self._lib.cunfft_x_adjoint(self._h, _ptr(f), _ptr(fh)), self._h)
         return fh
+
+    # ------------------------------------------------ host buffers, overlapped copies
+    def _host(self, t, dtype, numel, what):
+        if t.is_cuda or t.dtype != dtype or not t.is_contiguous() or t.numel() != numel:
+            raise ValueError(f"{what} must be a contiguous CPU {dtype} tensor of {numel} elements (pinned for overlap)")
+        return t
+
+    def forward_host(self, fhat, out, x=None, M_inst=None):
+        """Forward transform between CPU tensors with the copies overlapped with the
+        plan's kernels: x (float64, sum M_i x d; None keeps the bound nodes), fhat in,
+        out (samples) written.  Asynchronous: keep the tensors alive and the inputs
+        unchanged until synchronize(); pin them (tensor.pin_memory()) for overlap."""
+        arr = None
+        if x is not None:
+            M = x.numel() // self.d
+            self._host(x, torch.float64, M * self.d, "x")
+            if M_inst is None:
+                if self.batch != 1:
+                    raise ValueError("M_inst is required for batched plans")
+                M_inst = [M]
+            M_inst = [int(v) for v in M_inst]
+            if len(M_inst) != self.batch or sum(M_inst) != M:
+                raise ValueError("M_inst must have one count per instance summing to the node count")
+            arr = (ctypes.c_int64 * self.batch)(*M_inst)
+            self.M_inst, self.M, self.x = M_inst, M, None
+        self._host(fhat, self.cdtype, self.batch * self.N_total, "fhat")
+        self._host(out, self.cdtype, self.M, "out")
+        nat.check(self._lib.cunfft_x_forward_host(self._h, _ptr(x), arr, _ptr(fhat), _ptr(out)), self._h)
+        self._host_refs.extend([x, fhat, out])
+        return out
+
+    def adjoint_host(self, f, out):
+        """Adjoint between CPU tensors on the bound nodes (see forward_host)."""
+        self._host(f, self.cdtype, self.M, "f")
+        self._host(out, self.cdtype, self.batch * self.N_total, "out")
+        nat.check(self._lib.cunfft_x_adjoint_host(self._h, _ptr(f), _ptr(out)), self._h)
+        self._host_refs.extend([f, out])
+        return out
 
     def forward_graph(self, fhat, out):
         """forward() replayed from a captured CUDA graph (fixed buffers fhat, out)."""
@@ -212,6 +251,7 @@ class NFFT:
 
     def synchronize(self):
         nat.check(self._lib.cunfft_x_synchronize(self._h), self._h)
+        self._host_refs = []  # host buffers of finished host-buffer transforms
 
     def grid(self):
         """The plan's oversampled grid as a tensor view (batch, *n)."""

@@ -184,8 +184,23 @@ int cunfft_x_get_interp_kernel(const cunfft_x_plan *plan, int *kind);
  *  (binning, roll-off, FFT, gridding).  Blocks until the plan stream is idle. */
 int cunfft_x_stage_times(cunfft_x_plan *plan, double *t_bin, double *t_roc, double *t_fft, double *t_conv);
 
-/** Block until the plan's stream is idle; reports asynchronous errors and
- *  device-side check failures (CUNFFT_X_DEVICE_CHECK_FAILED, flag cleared on read). */
+/** Forward transform between host buffers, with the copies on the plan's two copy
+ *  streams overlapped with its kernels (the reference copies synchronously around
+ *  every transform, src/cunfft.cu:107-190).  x_host (sum M[i] x d doubles) with the
+ *  per-instance counts M rebinds the nodes first; x_host = NULL keeps the bound
+ *  nodes.  fhat_host (batch x N_total complex) in, f_host (sum M complex) out.
+ *  Asynchronous: host buffers should be pinned, must stay valid and the inputs
+ *  unchanged until cunfft_x_synchronize(plan), which also waits for the copies. */
+int cunfft_x_forward_host(cunfft_x_plan *plan, const double *x_host, const int64_t *M, const void *fhat_host,
+                          void *f_host);
+
+/** Adjoint between host buffers on the bound nodes: f_host in, fhat_host out; same
+ *  rules as cunfft_x_forward_host.  Its upload overlaps a preceding forward. */
+int cunfft_x_adjoint_host(cunfft_x_plan *plan, const void *f_host, void *fhat_host);
+
+/** Block until the plan's stream (and the copy streams of the host-buffer
+ *  transforms) are idle; reports asynchronous errors and device-side check
+ *  failures (CUNFFT_X_DEVICE_CHECK_FAILED, flag cleared on read). */
 int cunfft_x_synchronize(cunfft_x_plan *plan);
 
 /** Last error message of a plan (empty string when none). */
