@@ -58,7 +58,7 @@ __host__ __device__ constexpr int fixed_plane_stride(int d, int W) {
 // Tiling of the oversampled grid used by the gridding kernels.
 struct Tiling {
   int T[kMaxDim];        // tile extent per dim (power of two, <= n_t)
-  int nb[kMaxDim];       // tiles per dim = n_t / T_t
+  int nb[kMaxDim];       // tiles per dim = ceil(n_t / T_t)
   int E[kMaxDim];        // padded extent per dim = T_t + W - 1
   int S;                 // shared-memory row stride (elements) for the innermost dim
   int R1;                // rows per plane (E[d-2] for d = 3, unused otherwise)
@@ -92,6 +92,19 @@ struct Bins {
   int      valid;        // nodes binned for the current tiling
 };
 
-__host__ __device__ inline int64_t wrap_pow2(int64_t i, int64_t n) { return i & (n - 1); }
+// i mod n in [0, n) for any i: a mask when n is a power of two, else the remainder.
+__host__ __device__ inline int64_t wrap_n(int64_t i, int64_t n) {
+  if ((n & (n - 1)) == 0) return i & (n - 1);
+  const int64_t r = i % n;
+  return r < 0 ? r + n : r;
+}
+
+// i mod n for 0 <= i: tile origin plus an offset inside the padded tile, at most one
+// tile extent past n except on grids smaller than the tile; no division.
+__host__ __device__ __forceinline__ int64_t wrap_up(int64_t i, int64_t n) {
+  if ((n & (n - 1)) == 0) return i & (n - 1);
+  while (i >= n) i -= n;
+  return i;
+}
 
 }  // namespace cg

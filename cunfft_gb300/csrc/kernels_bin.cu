@@ -39,7 +39,7 @@ __global__ void k_bin_count(const double* __restrict__ x, int64_t M, Geom geo, T
     for (int t = 0; t < d; ++t) {
       int64_t u; double c;
       reduce_coord(x[j * d + t], geo.n[t], geo.m, u, c);
-      int64_t s = wrap_pow2(u, geo.n[t]);
+      int64_t s = wrap_n(u, geo.n[t]);
       tile = tile * tl.nb[t] + (s >> (__ffs(tl.T[t]) - 1));  // T_t is a power of two
     }
     tile += (int64_t)inst * tl.tiles_per_inst;
@@ -60,7 +60,7 @@ __global__ void k_bin_scatter(const double* __restrict__ x, int64_t M, Geom geo,
     for (int t = 0; t < d; ++t) {
       int64_t u; double c;
       reduce_coord(x[j * d + t], geo.n[t], geo.m, u, c);
-      int64_t s = wrap_pow2(u, geo.n[t]);
+      int64_t s = wrap_n(u, geo.n[t]);
       uint32_t o = (uint32_t)(s & (tl.T[t] - 1));  // T_t is a power of two
       packed |= o << (off_bits_host(d) * t);
       sfrac[pos * d + t] = (T)(c - (double)geo.m);

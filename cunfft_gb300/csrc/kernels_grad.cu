@@ -55,13 +55,13 @@ __global__ void __launch_bounds__(128) k_interp_grad(const double* __restrict__ 
     // partial sums: p[t] = sum g * (derivative in dim t, plain weights elsewhere)
     T pr[kMaxDim] = {0, 0, 0}, pi[kMaxDim] = {0, 0, 0};
     for (int l0 = 0; l0 < W; ++l0) {
-      const int64_t i0 = wrap_pow2(u[0] + l0, geo.n[0]);
+      const int64_t i0 = wrap_n(u[0] + l0, geo.n[0]);
       for (int l1 = 0; l1 < W1; ++l1) {
-        const int64_t i1 = d >= 2 ? wrap_pow2(u[1] + l1, geo.n[1]) : 0;
+        const int64_t i1 = d >= 2 ? wrap_n(u[1] + l1, geo.n[1]) : 0;
         // inner sums over the last dimension: plain and derivative weights
         T ar = 0, ai = 0, br = 0, bi = 0;
         for (int l2 = 0; l2 < W2; ++l2) {
-          const int64_t i2 = d >= 3 ? wrap_pow2(u[2] + l2, geo.n[2]) : 0;
+          const int64_t i2 = d >= 3 ? wrap_n(u[2] + l2, geo.n[2]) : 0;
           int64_t gidx = i0;
           if (d >= 2) gidx = gidx * geo.n[1] + i1;
           if (d >= 3) gidx = gidx * geo.n[2] + i2;

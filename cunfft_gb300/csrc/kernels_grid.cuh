@@ -180,8 +180,8 @@ __device__ __forceinline__ void row_coords(const Tiling& tl, int row, int* p0, i
 
 template <int D>
 __device__ __forceinline__ int64_t row_gbase(const Geom& geo, const TileOrigin& o, int p0, int p1) {
-  if (D == 3) return (wrap_pow2(o.a[0] + p0, geo.n[0]) * geo.n[1] + wrap_pow2(o.a[1] + p1, geo.n[1])) * geo.n[2];
-  if (D == 2) return wrap_pow2(o.a[0] + p0, geo.n[0]) * geo.n[1];
+  if (D == 3) return (wrap_up(o.a[0] + p0, geo.n[0]) * geo.n[1] + wrap_up(o.a[1] + p1, geo.n[1])) * geo.n[2];
+  if (D == 2) return wrap_up(o.a[0] + p0, geo.n[0]) * geo.n[1];
   return 0;
 }
 
@@ -192,7 +192,7 @@ __device__ __forceinline__ void load_tile(C* tile, const C* __restrict__ gi, con
   const int E_last = tl.E[D - 1];
   const int64_t n_last = geo.n[D - 1], a_last = o.a[D - 1];
   if (D == 1) {
-    for (int p = threadIdx.x; p < E_last; p += blockDim.x) cp_async_elem(tile + p, gi + wrap_pow2(a_last + p, n_last));
+    for (int p = threadIdx.x; p < E_last; p += blockDim.x) cp_async_elem(tile + p, gi + wrap_up(a_last + p, n_last));
     cp_async_wait_all();
     return;
   }
@@ -203,13 +203,13 @@ __device__ __forceinline__ void load_tile(C* tile, const C* __restrict__ gi, con
     row_coords<D>(tl, row, &p0, &p1);
     const int64_t gbase = row_gbase<D>(geo, o, p0, p1);
     C* dst = tile + (D == 3 ? p0 * PS + p1 * S : p0 * S);
-    for (int p = lane; p < E_last; p += kWarp) cp_async_elem(dst + p, gi + gbase + wrap_pow2(a_last + p, n_last));
+    for (int p = lane; p < E_last; p += kWarp) cp_async_elem(dst + p, gi + gbase + wrap_up(a_last + p, n_last));
   }
   cp_async_wait_all();  // this thread's copies landed; the caller's barrier publishes them
 }
 
-// Add the tile into the global grid.  FP32 pairs (even offset, so 16-byte
-// aligned and never split by the power-of-two wrap) go as one float4 atomic.
+// Add the tile into the global grid.  FP32 pairs (even offset on a grid whose last
+// size is even, so 16-byte aligned and never split by the wrap) go as one float4 atomic.
 template <int D, int W, typename C>
 __device__ __forceinline__ void flush_tile(const C* tile, C* __restrict__ gi, const Geom& geo, const Tiling& tl,
                                            const TileOrigin& o) {
@@ -219,7 +219,7 @@ __device__ __forceinline__ void flush_tile(const C* tile, C* __restrict__ gi, co
   const int rows = tile_rows<D>(tl);
   constexpr bool kF32 = sizeof(C) == 8;
   const int tid = threadIdx.x, nt = blockDim.x;
-  const bool pairs_ok = kF32 && n_last >= 2 && (tl.T[D - 1] & 1) == 0;  // even tile origin
+  const bool pairs_ok = kF32 && (n_last & 1) == 0 && (tl.T[D - 1] & 1) == 0;  // even tile origin and row length
   const int per_row = pairs_ok ? (E_last + 1) >> 1 : E_last;
   const int total = rows * per_row;
   for (int e = tid; e < total; e += nt) {
@@ -231,7 +231,7 @@ __device__ __forceinline__ void flush_tile(const C* tile, C* __restrict__ gi, co
     if (pairs_ok) {
       const int p = 2 * k;
       const C v0 = src[p];
-      const int64_t gidx = gb + wrap_pow2(a_last + p, n_last);
+      const int64_t gidx = gb + wrap_up(a_last + p, n_last);
       if (p + 1 < E_last) {
         const C v1 = src[p + 1];
         if (v0.x != 0 || v0.y != 0 || v1.x != 0 || v1.y != 0)
@@ -241,7 +241,7 @@ __device__ __forceinline__ void flush_tile(const C* tile, C* __restrict__ gi, co
       }
     } else {
       const C v = src[k];
-      if (v.x != 0 || v.y != 0) global_add(gi + gb + wrap_pow2(a_last + k, n_last), v);
+      if (v.x != 0 || v.y != 0) global_add(gi + gb + wrap_up(a_last + k, n_last), v);
     }
   }
 }

@@ -37,7 +37,7 @@ __global__ void __launch_bounds__(128) k_grid_global(const typename Cx<T>::t* __
         acc.x = (T)0;
         acc.y = (T)0;
         for (int l0 = 0; l0 < W; ++l0) {
-          const int64_t i0 = wrap_pow2(s[0] + l0, geo.n[0]);
+          const int64_t i0 = wrap_up(s[0] + l0, geo.n[0]);
           if (D == 1) {
             acc = cmul_add(acc, w[0][l0], in[inst_base + i0]);
             continue;
@@ -46,7 +46,7 @@ __global__ void __launch_bounds__(128) k_grid_global(const typename Cx<T>::t* __
           a1.x = (T)0;
           a1.y = (T)0;
           for (int l1 = 0; l1 < W; ++l1) {
-            const int64_t i1 = wrap_pow2(s[1] + l1, geo.n[1]);
+            const int64_t i1 = wrap_up(s[1] + l1, geo.n[1]);
             if (D == 2) {
               a1 = cmul_add(a1, w[1][l1], in[inst_base + i0 * geo.n[1] + i1]);
               continue;
@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(128) k_grid_global(const typename Cx<T>::t* __
             a2.y = (T)0;
             const int64_t rowb = inst_base + (i0 * geo.n[1] + i1) * geo.n[D - 1];
             for (int l2 = 0; l2 < W; ++l2)
-              a2 = cmul_add(a2, w[D - 1][l2], in[rowb + wrap_pow2(s[D - 1] + l2, geo.n[D - 1])]);
+              a2 = cmul_add(a2, w[D - 1][l2], in[rowb + wrap_up(s[D - 1] + l2, geo.n[D - 1])]);
             a1 = cmul_add(a1, w[1][l1], a2);
           }
           acc = cmul_add(acc, w[0][l0], a1);
@@ -65,14 +65,14 @@ __global__ void __launch_bounds__(128) k_grid_global(const typename Cx<T>::t* __
       } else {
         const C v = cscale(in[idx], norm);
         for (int l0 = 0; l0 < W; ++l0) {
-          const int64_t i0 = wrap_pow2(s[0] + l0, geo.n[0]);
+          const int64_t i0 = wrap_up(s[0] + l0, geo.n[0]);
           const C v0 = cscale(v, w[0][l0]);
           if (D == 1) {
             global_add(&out[inst_base + i0], v0);
             continue;
           }
           for (int l1 = 0; l1 < W; ++l1) {
-            const int64_t i1 = wrap_pow2(s[1] + l1, geo.n[1]);
+            const int64_t i1 = wrap_up(s[1] + l1, geo.n[1]);
             const C v1 = cscale(v0, w[1][l1]);
             if (D == 2) {
               global_add(&out[inst_base + i0 * geo.n[1] + i1], v1);
@@ -80,7 +80,7 @@ __global__ void __launch_bounds__(128) k_grid_global(const typename Cx<T>::t* __
             }
             const int64_t rowb = inst_base + (i0 * geo.n[1] + i1) * geo.n[D - 1];
             for (int l2 = 0; l2 < W; ++l2)
-              global_add(&out[rowb + wrap_pow2(s[D - 1] + l2, geo.n[D - 1])], cscale(v1, w[D - 1][l2]));
+              global_add(&out[rowb + wrap_up(s[D - 1] + l2, geo.n[D - 1])], cscale(v1, w[D - 1][l2]));
           }
         }
       }

@@ -44,7 +44,7 @@ __host__ __device__ constexpr int it_n(int W) { return (it_ncol(W) + 15) / 16 * 
 __host__ __device__ constexpr int it_pairs_pad(int W) { return (it_ch(W) * it_e1(W) + 7) / 8 * 8; }
 
 __host__ __device__ constexpr bool interp_tc_ok(int d, int W, int T0, int64_t n2) {
-  return d == 3 && W >= 4 && W <= 16 && T0 >= 1 && T0 <= kItMaxT0 && n2 >= 4;
+  return d == 3 && W >= 4 && W <= 16 && T0 >= 1 && T0 <= kItMaxT0 && n2 >= 4 && n2 % 4 == 0;
 }
 
 // Shared-memory layout (byte offsets; host and device agree).
@@ -188,13 +188,13 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const float2* __res
             const int pl = pair / E1, p1 = pair - pl * E1;
             const bool on = pl < np;
             int64_t rowg = 0;
-            if (on) rowg = (wrap_pow2(o.a[0] + ps + pl, n0) * n1 + wrap_pow2(o.a[1] + p1, n1)) * n2;
+            if (on) rowg = (wrap_up(o.a[0] + ps + pl, n0) * n1 + wrap_up(o.a[1] + p1, n1)) * n2;
 #pragma unroll
             for (int qh = 0; qh < 2; ++qh) {
               const int qd = qh * 4 + qq;  // p2 = 4 qd .. 4 qd + 3 (never straddles the wrap: n2 % 4 == 0)
               v[i][qh][0] = v[i][qh][1] = make_float4(0.f, 0.f, 0.f, 0.f);
               if (on) {
-                const float4* src = reinterpret_cast<const float4*>(gi + rowg + wrap_pow2(o.a[2] + 4 * qd, n2));
+                const float4* src = reinterpret_cast<const float4*>(gi + rowg + wrap_up(o.a[2] + 4 * qd, n2));
                 v[i][qh][0] = src[0];
                 v[i][qh][1] = src[1];
               }

@@ -12,7 +12,7 @@
 
 namespace cg {
 
-// log2 of the power-of-two grid sizes, computed on the host
+// log2 of the grid sizes when every one is a power of two, computed on the host
 struct RocShifts {
   int lg_n[kMaxDim];
   int lg_ntot;
@@ -28,10 +28,10 @@ __device__ __forceinline__ int64_t roc_slot(int64_t i, int64_t N, int64_t n) {
 }
 
 // EPT consecutive grid points per thread (2 when the last grid size is even, so a
-// pair never leaves its row; 1 otherwise); integer decoding by shifts only, and the
-// FP64 factor product, in the order dimension 0, 1, ..., only for points inside I_N
-// (one in 2^d of the grid).
-template <typename T, int EPT>
+// pair never leaves its row; 1 otherwise); integer decoding by shifts and masks when
+// every grid size is a power of two (P2), by division otherwise, and the FP64 factor
+// product, in the order dimension 0, 1, ..., only for points inside I_N.
+template <typename T, int EPT, bool P2>
 __global__ void k_roc_forward(const typename Cx<T>::t* __restrict__ fhat, typename Cx<T>::t* __restrict__ g,
                               Geom geo, const double* __restrict__ tab, RocShifts sh) {
   using C = typename Cx<T>::t;
@@ -41,14 +41,21 @@ __global__ void k_roc_forward(const typename Cx<T>::t* __restrict__ fhat, typena
   for (int64_t e2 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e2 < total2;
        e2 += (int64_t)gridDim.x * blockDim.x) {
     const int64_t e = EPT * e2;
-    const int64_t inst = e >> sh.lg_ntot, gi = e & (geo.ntot - 1);
-    const int64_t i_last = gi & (n_last - 1);
-    int64_t rest = gi >> sh.lg_n[d - 1];
+    const int64_t inst = P2 ? e >> sh.lg_ntot : e / geo.ntot;
+    const int64_t gi = P2 ? e & (geo.ntot - 1) : e - inst * geo.ntot;
+    const int64_t i_last = P2 ? gi & (n_last - 1) : gi % n_last;
+    int64_t rest = P2 ? gi >> sh.lg_n[d - 1] : gi / n_last;
     // leading dimensions 0 .. d-2
     int64_t lead_idx[kMaxDim];
     for (int t = d - 2; t >= 0; --t) {
-      lead_idx[t] = rest & (geo.n[t] - 1);
-      rest >>= sh.lg_n[t];
+      if (P2) {
+        lead_idx[t] = rest & (geo.n[t] - 1);
+        rest >>= sh.lg_n[t];
+      } else {
+        const int64_t q = rest / geo.n[t];
+        lead_idx[t] = rest - q * geo.n[t];
+        rest = q;
+      }
     }
     bool lead_in = true;
     int64_t ci = 0, tab_base = 0;
@@ -103,7 +110,7 @@ __global__ void k_roc_adjoint(const typename Cx<T>::t* __restrict__ g, typename 
     int64_t gidx = 0, tab_base = 0;
     for (int t = 0; t < d; ++t) {
       const int64_t k = (int64_t)c[t] - geo.N[t] / 2;
-      gidx = gidx * geo.n[t] + (k & (geo.n[t] - 1));
+      gidx = gidx * geo.n[t] + (k < 0 ? k + geo.n[t] : k);  // |k| <= N_t / 2 <= n_t / 2
       fac *= tab[tab_base + c[t]];
       tab_base += geo.N[t];
     }
@@ -114,6 +121,12 @@ __global__ void k_roc_adjoint(const typename Cx<T>::t* __restrict__ g, typename 
     out.y = a.y * s;
     fhat[e] = out;
   }
+}
+
+static bool all_pow2(const Geom& geo) {
+  for (int t = 0; t < kMaxDim; ++t)
+    if ((geo.n[t] & (geo.n[t] - 1)) != 0) return false;
+  return true;
 }
 
 static RocShifts roc_shifts(const Geom& geo) {
@@ -135,19 +148,26 @@ static inline int roc_grid(const Plan& p, int64_t work) {
   return (int)(b > cap ? cap : (b < 1 ? 1 : b));
 }
 
+template <typename T>
+static cudaError_t launch_roc_fwd_t(const Plan& p, bool pairs, bool p2, int blocks, const void* fhat, void* g,
+                                   const RocShifts& sh, cudaStream_t st) {
+  using C = typename Cx<T>::t;
+  const C* in = (const C*)fhat;
+  C* out = (C*)g;
+  if (pairs && p2) k_roc_forward<T, 2, true><<<blocks, 256, 0, st>>>(in, out, p.geo, p.roc_tab, sh);
+  else if (pairs) k_roc_forward<T, 2, false><<<blocks, 256, 0, st>>>(in, out, p.geo, p.roc_tab, sh);
+  else if (p2) k_roc_forward<T, 1, true><<<blocks, 256, 0, st>>>(in, out, p.geo, p.roc_tab, sh);
+  else k_roc_forward<T, 1, false><<<blocks, 256, 0, st>>>(in, out, p.geo, p.roc_tab, sh);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_roc_forward(const Plan& p, const void* fhat, void* g, cudaStream_t st) {
   const bool pairs = (p.geo.n[p.geo.d - 1] & 1) == 0;
   const int64_t work = p.geo.ntot * p.geo.batch / (pairs ? 2 : 1);
   const RocShifts sh = roc_shifts(p.geo);
   const int blocks = roc_grid(p, work);
-  if (p.prec == kF64) {
-    if (pairs) k_roc_forward<double, 2><<<blocks, 256, 0, st>>>((const double2*)fhat, (double2*)g, p.geo, p.roc_tab, sh);
-    else k_roc_forward<double, 1><<<blocks, 256, 0, st>>>((const double2*)fhat, (double2*)g, p.geo, p.roc_tab, sh);
-  } else {
-    if (pairs) k_roc_forward<float, 2><<<blocks, 256, 0, st>>>((const float2*)fhat, (float2*)g, p.geo, p.roc_tab, sh);
-    else k_roc_forward<float, 1><<<blocks, 256, 0, st>>>((const float2*)fhat, (float2*)g, p.geo, p.roc_tab, sh);
-  }
-  return cudaGetLastError();
+  if (p.prec == kF64) return launch_roc_fwd_t<double>(p, pairs, all_pow2(p.geo), blocks, fhat, g, sh, st);
+  return launch_roc_fwd_t<float>(p, pairs, all_pow2(p.geo), blocks, fhat, g, sh, st);
 }
 
 cudaError_t launch_roc_adjoint(const Plan& p, const void* g, void* fhat, cudaStream_t st) {

@@ -382,6 +382,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spread_tc(const float2* __res
     const int q = warp - kTcEpiWarp0;
     const int64_t n0 = geo.n[0], n1 = geo.n[1], n2 = geo.n[2];
     const int E1a = tl.E[1], E2a = tl.E[2];
+    const bool one_wrap = n2 >= E2a;
     uint32_t k = 0;
     int4 nxt = (int)blockIdx.x < num_items ? bins.items[blockIdx.x] : make_int4(0, 0, 0, 0);
     for (int it = blockIdx.x; it < num_items; it += G) {
@@ -394,11 +395,16 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spread_tc(const float2* __res
       __syncwarp();
       tc::fence_after_sync();
       const uint32_t acc = tmem + a * (uint32_t)(L.mt * kTcN) + ((uint32_t)(32 * q) << 16);
+      // columns: a2 + p2 wraps at most once when the row is at least as long as the
+      // padded tile (then p2 >= kw wraps); shorter rows take the general wrap
+      const int kw = (int)(n2 - o.a[2] < 64 ? n2 - o.a[2] : 64);
       for (int mt = 0; mt < L.mt; ++mt) {
         const int r = mt * 128 + 32 * q + lane;
         const int p0 = r / E1, p1 = r - p0 * E1;
         const bool row_on = r < rows && p1 < E1a;
-        const int64_t rbase = (wrap_pow2(o.a[0] + p0, n0) * n1 + wrap_pow2(o.a[1] + p1, n1)) * n2;
+        const int64_t rbase = (wrap_up(o.a[0] + p0, n0) * n1 + wrap_up(o.a[1] + p1, n1)) * n2;
+        float2* const rowa = gi + rbase + o.a[2];
+        float2* const roww = rowa - n2;
 #pragma unroll 1
         for (int c = 0; c < kTcN / 16; ++c) {
           float v[16];
@@ -409,15 +415,17 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spread_tc(const float2* __res
             for (int u = 0; u < 4; ++u) {
               const int p2 = c * 8 + 2 * u;  // pair (p2, p2 + 1): columns 4u .. 4u + 3 of this load
               if (p2 < E2a) {
-                float2* dst = gi + rbase + wrap_pow2(o.a[2] + p2, n2);
+                float2* dst = one_wrap ? (p2 >= kw ? roww : rowa) + p2 : gi + rbase + wrap_up(o.a[2] + p2, n2);
                 const float4 w = make_float4(v[4 * u], v[4 * u + 1], v[4 * u + 2], v[4 * u + 3]);
-                if (p2 + 1 < E2a && n2 >= 2) {
+                if (p2 + 1 < E2a && (n2 & 1) == 0) {  // even row length: the pair is 16-byte aligned
                   if (w.x != 0.f || w.y != 0.f || w.z != 0.f || w.w != 0.f)
                     atomicAdd(reinterpret_cast<float4*>(dst), w);
                 } else {
                   if (w.x != 0.f || w.y != 0.f) atomicAdd(dst, make_float2(w.x, w.y));
                   if (p2 + 1 < E2a && (w.z != 0.f || w.w != 0.f))
-                    atomicAdd(gi + rbase + wrap_pow2(o.a[2] + p2 + 1, n2), make_float2(w.z, w.w));
+                    atomicAdd(one_wrap ? (p2 + 1 >= kw ? roww : rowa) + (p2 + 1)
+                                       : gi + rbase + wrap_up(o.a[2] + p2 + 1, n2),
+                              make_float2(w.z, w.w));
                 }
               }
             }

@@ -83,7 +83,7 @@ static Tiling make_tiling(const Plan* p, const int* T, int chunk) {
   Tiling tl{};
   for (int t = 0; t < kMaxDim; ++t) {
     tl.T[t] = t < d ? T[t] : 1;
-    tl.nb[t] = t < d ? (int)(p->geo.n[t] / T[t]) : 1;
+    tl.nb[t] = t < d ? (int)((p->geo.n[t] + T[t] - 1) / T[t]) : 1;  // the last tile may be partial
     tl.E[t] = t < d ? T[t] + W - 1 : 1;
   }
   // inner strides are the kernels' compile-time values (inner tiles may be
@@ -151,7 +151,7 @@ int plan_choose_tiling(Plan* p, const int* Tin, int chunk) {
     T[0] = Tin[0];
   }
   for (int t = 0; t < d; ++t)
-    if (T[t] > p->geo.n[t]) T[t] = (int)p->geo.n[t];
+    while (T[t] > p->geo.n[t]) T[t] >>= 1;  // powers of two, at most the grid size
   Tiling tl = make_tiling(p, T, chunk);
   while (smem_of(p, tl) > kMaxSmem && T[0] > 1) {
     T[0] /= 2;
@@ -160,7 +160,7 @@ int plan_choose_tiling(Plan* p, const int* Tin, int chunk) {
   if (smem_of(p, tl) > kMaxSmem) {
     default_tiles(p, T);
     for (int t = 0; t < d; ++t)
-      if (T[t] > p->geo.n[t]) T[t] = (int)p->geo.n[t];
+      while (T[t] > p->geo.n[t]) T[t] >>= 1;
     tl = make_tiling(p, T, chunk);
     tl.use_global = 1;
     tl.threads = 128;
@@ -235,8 +235,6 @@ int geom_init(Plan* p, int d, const int64_t* N, const int64_t* n, int m, int pre
       while (nt < N[t]) nt <<= 1;
       nt *= 2;
     }
-    if (!is_pow2(nt))
-      return set_status(p, CUNFFT_X_UNSUPPORTED, "n[%d] = %lld is not a power of two", t, (long long)nt);
     if (nt < N[t]) return set_status(p, CUNFFT_X_INVALID_ARGUMENT, "n[%d] < N[%d]", t, t);
     g.N[t] = N[t];
     g.n[t] = nt;

@@ -64,9 +64,14 @@ enum cunfft_x_status {
 
 typedef struct cunfft_x_plan cunfft_x_plan;
 
-/** Create a plan.  d in 1..3; N[d] bandwidths; n[d] oversampled grid sizes
- *  (powers of two with n_t >= N_t; NULL selects n_t = 2*next_pow2(N_t) like
- *  cunfft_init, src/cunfft.cu:296-299); 1 <= m <= 15; precision CUNFFT_X_F64 or
+/** Create a plan.  d in 1..3; N[d] bandwidths (any N_t >= 1, odd included:
+ *  frequencies k_t in [-floor(N_t/2), N_t - floor(N_t/2))); n[d] oversampled grid
+ *  sizes, any n_t >= N_t (NULL selects n_t = 2*next_pow2(N_t) like cunfft_init,
+ *  src/cunfft.cu:296-299).  The reference wraps window indices with &(n-1)
+ *  (src/cunfft_kernel.cu:590, :768, :1036), so there n must be a power of two;
+ *  here any size wraps correctly.  The tensor-core gridding forms need 3D with an
+ *  even last size (spreading) or one divisible by 4 (interpolation); other
+ *  sizes run the shared-tile forms.  1 <= m <= 15; precision CUNFFT_X_F64 or
  *  CUNFFT_X_F32; batch >= 1 instances; stream 0 creates a private stream
  *  (a cudaStream_t may be passed as void*). */
 int cunfft_x_plan_create(cunfft_x_plan **plan, int d, const int64_t *N, const int64_t *n, int m,

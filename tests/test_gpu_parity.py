@@ -396,7 +396,7 @@ def test_errors_are_status_codes(dev):
     from cunfft_gb300.nfft import NFFT
 
     with pytest.raises(nat.CunfftError):
-        NFFT([10], n=[24], device=dev)  # n not a power of two
+        NFFT([10], n=[8], device=dev)  # n < N
     with pytest.raises(nat.CunfftError):
         NFFT([10], m=16, device=dev)
     p = NFFT([16], device=dev)

@@ -136,3 +136,22 @@ def test_oracle_odd_and_small_grids():
         ref = O.ndft_forward(x, fh, N)
         got = O.nfft_forward(x, fh, N, m=m)
         assert O.rel_l2(ref, got) < 5e-3
+
+
+@pytest.mark.parametrize("N,n", [([10], [24]), ([31], [45]), ([12, 20], [24, 50]), ([15, 9], [30, 27]),
+                                 ([6, 5, 7], [12, 15, 14])])
+def test_oracle_general_grid_sizes(N, n):
+    """Non-power-of-two oversampled grids (true modulo wrap, direct DFT on those lengths):
+    the NFFT pair stays an accurate approximation of the NDFT pair and stays adjoint."""
+    rng = np.random.default_rng(sum(n))
+    M = 60
+    x = rng.uniform(-0.5, 0.5, (M, len(N)))
+    fh = rng.standard_normal(N) + 1j * rng.standard_normal(N)
+    f = rng.standard_normal(M) + 1j * rng.standard_normal(M)
+    sigma = min(a / b for a, b in zip(n, N))
+    tol = 1e-5 if sigma >= 2 else 1e-3
+    assert O.rel_l2(O.ndft_forward(x, fh, N), O.nfft_forward(x, fh, N, n=n)) < tol
+    assert O.rel_l2(O.ndft_adjoint(x, f, N), O.nfft_adjoint(x, f, N, n=n)) < tol
+    lhs = np.vdot(f, O.nfft_forward(x, fh, N, n=n))
+    rhs = np.vdot(O.nfft_adjoint(x, f, N, n=n), fh)
+    assert abs(lhs - rhs) < 1e-10 * abs(lhs)
