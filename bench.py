@@ -12,7 +12,9 @@ value = M * n_gpus / (time per step), max over ranks.  ``value`` is the FP32
 form (FP32 gridding, FFT and accumulation; FP64 node reduction and roll-off);
 the FP64 form (the reference's arithmetic) is timed in the same run and
 reported as ``fp64_plain``.  Errors are relative l2 against the FP64 direct
-NDFT on a 4096-node subsample (forward) and 4096 coefficients (adjoint).
+NDFT on a 4096-node subsample (forward) and 4096 coefficients (adjoint).  The
+same step with the ES window of the extension API (cunfft_x_set_window) is
+timed and checked in both forms and reported as ``es_window``.
 
 ``--impl reference`` times the reference method on the host CPU cores instead
 (the CPU restatement in oracle/, OpenMP over all host threads; the reference
@@ -365,6 +367,36 @@ def run_ours(args):
            "fp64_forward": rel_l2(nd_f, r64f), "fp64_adjoint": rel_l2(nd_h, r64h)}
     sub.close()
 
+    # ---------------- ES window (cunfft_x_set_window): same step, same NDFT subsamples ----------------
+    p64.set_window("es")
+    p32.set_window("es")
+    step64()
+    barrier()
+    e0.record(stream)
+    for _ in range(k64):
+        step64()
+    e1.record(stream)
+    barrier()
+    ms64_es = max_over_ranks(e0.elapsed_time(e1) / k64)
+    step32()
+    barrier()
+    e0.record(stream)
+    for _ in range(args.steps):
+        step32()
+    e1.record(stream)
+    barrier()
+    ms32_es = max_over_ranks(e0.elapsed_time(e1) / args.steps)
+    es = {"window": "exponential of semicircle, alpha = m + 1/2, beta = 0.97 pi (2m+1)(1 - 1/(2 sigma))",
+          "fp32": {"value": replica_points_per_s(M, world, ms32_es), "ms_per_step": ms32_es,
+                   "rel_l2_vs_ndft": {"forward": rel_l2(nd_f, p32.forward(fh32)[idx]),
+                                      "adjoint": rel_l2(nd_h, p32.adjoint(f32).reshape(-1)[kidx])}},
+          "fp64": {"value": replica_points_per_s(M, world, ms64_es), "ms_per_step": ms64_es, "steps": k64,
+                   "rel_l2_vs_ndft": {"forward": rel_l2(nd_f, o64f[idx]), "adjoint": rel_l2(nd_h, o64h.reshape(-1)[kidx])}},
+          "ratio_fp32_vs_fp64": ms64_es / ms32_es}
+    p64.set_window("gaussian")
+    p32.set_window("gaussian")
+    p32.set_nodes(x)
+
     # ---------------- end to end through the C ABI from pinned host buffers ----------------
     # cunfft_x_forward_host / cunfft_x_adjoint_host: nodes, coefficients and samples
     # upload and download on the plan's two copy streams, overlapped with its kernels;
@@ -412,6 +444,7 @@ def run_ours(args):
                               "step": "forward + adjoint on an already-binned node set"},
         "fp64_plain": {"value": replica_points_per_s(M, world, ms64), "ms_per_step": ms64, "steps": k64},
         "ratio_fp32_vs_fp64": ms64 / ms32_max,
+        "es_window": es,
         "rel_l2_vs_ndft": err,
         "stages_fp32": stages32,
         "e2e": {"value": replica_points_per_s(M, world, ms_e2e), "unit": UNIT, "h2d_bytes_per_step": h2d,

@@ -85,6 +85,7 @@ X_SYMBOLS = [
     "cunfft_x_autotune", "cunfft_x_get_tiling", "cunfft_x_stage_times", "cunfft_x_synchronize",
     "cunfft_x_last_message", "cunfft_x_status_string", "cunfft_x_grid", "cunfft_x_version",
     "cunfft_x_spread_noalloc", "cunfft_x_set_spread_kernel", "cunfft_x_get_spread_kernel",
+    "cunfft_x_set_window", "cunfft_x_get_window",
     "cunfft_x_set_interp_kernel", "cunfft_x_get_interp_kernel", "cunfft_x_forward_host", "cunfft_x_adjoint_host",
 ]
 UTIL_SYMBOLS = [
@@ -131,6 +132,8 @@ def lib():
         "cunfft_x_autotune": (ctypes.c_int, [vp, ctypes.c_int]),
         "cunfft_x_get_tiling": (ctypes.c_int, [vp, ip, ip, ip]),
         "cunfft_x_set_spread_kernel": (ctypes.c_int, [vp, ctypes.c_int]),
+        "cunfft_x_set_window": (ctypes.c_int, [vp, ctypes.c_int]),
+        "cunfft_x_get_window": (ctypes.c_int, [vp, ip]),
         "cunfft_x_get_spread_kernel": (ctypes.c_int, [vp, ip]),
         "cunfft_x_set_interp_kernel": (ctypes.c_int, [vp, ctypes.c_int]),
         "cunfft_x_get_interp_kernel": (ctypes.c_int, [vp, ip]),

@@ -30,12 +30,64 @@ struct Geom {
   int W;                 // taps per dimension, 2m+2
   int batch;             // number of instances
   int64_t N[kMaxDim];    // bandwidths (1 for unused dims)
-  int64_t n[kMaxDim];    // oversampled grid sizes, powers of two (1 for unused dims)
+  int64_t n[kMaxDim];    // oversampled grid sizes, any n_t >= N_t (1 for unused dims)
   int64_t Ntot, ntot;    // per instance
   double b[kMaxDim];     // Gaussian shape parameter per dim
-  double norm;           // prod_t sqrt(b'_t), b' = (2 sigma-1)/(2 sigma m) = 1/(pi b)
+  double norm;           // Gaussian: prod_t sqrt(b'_t), b' = (2 sigma-1)/(2 sigma m) = 1/(pi b); ES: 1
   float cbf[kMaxDim];    // log2(e) / b_t, rounded to FP32 (FP32 tap weights exp2(-y^2 cb))
+  // window: kWinGauss (the reference's) or kWinES, exponential of semicircle
+  // phi(y) = exp(beta_t (sqrt(1 - y^2 / alpha^2) - 1)) for |y| < alpha = m + 1/2, else 0
+  int window;
+  double es_beta[kMaxDim];  // beta_t
+  double es_ia2;            // 1 / alpha^2
+  float es_bl[kMaxDim];     // beta_t log2(e), FP32
+  float es_ia2f;            // 1 / alpha^2, FP32
 };
+
+constexpr int kWinGauss = 0;
+constexpr int kWinES = 1;
+
+// FP32 tap constants of one dimension: Gaussian exp2(-y^2 a); ES
+// exp2(-b q / (1 + sqrt(1 - q))), q = y^2 a (the ES exponent beta (sqrt(1 - q) - 1)
+// without the cancellation near the centre), zero for q >= 1.
+struct TapK {
+  float a, b;
+};
+// FP32 tap of the window at distance y (grid units) from the node
+template <int WIN>
+__device__ __forceinline__ float win_tap(float y, TapK k) {
+  if (WIN == kWinGauss) return exp2f(-(y * y) * k.a);
+  const float q = (y * y) * k.a, z = 1.f - q;
+  const float e = exp2f(__fdividef(-k.b * q, 1.f + z * rsqrtf(z)));  // NaN for z <= 0, not selected
+  return z > 0.f ? e : 0.f;
+}
+
+// tap constants of dimension t for a window fixed at compile time
+template <int WIN>
+__host__ __device__ inline TapK tap_k(const Geom& g, int t) {
+  TapK k;
+  if (WIN == kWinES) {
+    k.a = g.es_ia2f;
+    k.b = t == 0 ? g.es_bl[0] : (t == 1 ? g.es_bl[1] : g.es_bl[2]);
+  } else {
+    k.a = t == 0 ? g.cbf[0] : (t == 1 ? g.cbf[1] : g.cbf[2]);
+    k.b = 0.f;
+  }
+  return k;
+}
+
+// ... and for the plan's window
+__host__ __device__ inline TapK tap_k(const Geom& g, int t) {
+  TapK k;
+  if (g.window == kWinES) {
+    k.a = g.es_ia2f;
+    k.b = t == 0 ? g.es_bl[0] : (t == 1 ? g.es_bl[1] : g.es_bl[2]);
+  } else {
+    k.a = t == 0 ? g.cbf[0] : (t == 1 ? g.cbf[1] : g.cbf[2]);
+    k.b = 0.f;
+  }
+  return k;
+}
 
 // Compile-time extents of the inner tile dimensions of the shared-memory
 // gridding kernels (the outermost extent T0 stays a runtime, tunable value):

@@ -14,7 +14,7 @@ static cudaError_t launch_it(const Plan& p, const void* in, void* out, cudaStrea
   // SM's 228 KB of shared memory), so tcgen05.alloc never waits
   const ItLayout L = it_layout(W);
   const size_t smem = L.total > 116u * 1024u + 1u ? L.total : 116u * 1024u + 1u;
-  auto kern = k_interp_tc<W>;
+  auto kern = p.geo.window == kWinES ? k_interp_tc<W, kWinES> : k_interp_tc<W, kWinGauss>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int per_sm = 0;

@@ -25,7 +25,7 @@ template <int W>
 static cudaError_t launch_tc(const Plan& p, const void* in, void* out, cudaStream_t st) {
   if (!spread_tc_supported(p)) return cudaErrorInvalidConfiguration;
   const size_t smem = spread_tc_smem_bytes(p);
-  auto kern = k_spread_tc<W>;
+  auto kern = p.geo.window == kWinES ? k_spread_tc<W, kWinES> : k_spread_tc<W, kWinGauss>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int per_sm = 0;

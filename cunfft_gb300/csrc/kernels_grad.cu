@@ -1,8 +1,9 @@
-// kernels_grad.cu -- node-position gradient of the forward NFFT (derivative-of-Gaussian gridding).
+// kernels_grad.cu -- node-position gradient of the forward NFFT (derivative-of-window gridding).
 //
-// f_j = sum_l g[u + l] prod_t psi_t(c_t - l_t),  c_t = n_t x_t - u_t, psi(y) = K exp(-y^2/b), so
+// f_j = sum_l g[u + l] prod_t psi_t(c_t - l_t),  c_t = n_t x_t - u_t, so
 //   d f_j / d x_{j,t} = n_t sum_l g[u + l] psi_t'(c_t - l_t) prod_{s != t} psi_s(c_s - l_s),
-//   psi'(y) = -(2 y / b) psi(y).
+//   Gaussian psi(y) = K exp(-y^2/b): psi'(y) = -(2 y / b) psi(y);
+//   ES psi(y) = exp(beta (s - 1)), s = sqrt(1 - y^2/alpha^2): psi'(y) = -psi(y) beta y / (alpha^2 s).
 // The kernel evaluates the d partial derivatives on the same roll-off-corrected,
 // FFT'd grid g as the forward transform and contracts them with the incoming
 // gradient: grad_x[j, t] = Re(conj(grad_f_j) * d f_j / d x_{j,t}).
@@ -39,12 +40,24 @@ __global__ void __launch_bounds__(128) k_interp_grad(const double* __restrict__ 
       const double nx = __dmul_rn(xt, (double)geo.n[t]);
       u[t] = (int64_t)__double2ll_rn(nx) - (signbit(xt) ? 1 : 0) - geo.m;
       const double c = __dsub_rn(nx, (double)u[t]);
-      const double ib = 1.0 / geo.b[t];
-      for (int l = 0; l < W; ++l) {
-        const double y = c - (double)l;
-        const double e = exp(-(y * y) * ib);
-        w[t][l] = (T)e;
-        dw[t][l] = (T)(-2.0 * y * ib * e * (double)geo.n[t]);
+      if (geo.window == kWinES) {
+        // phi = exp(beta (s - 1)), s = sqrt(1 - y^2/alpha^2); dphi/dy = -phi beta y / (alpha^2 s)
+        const double beta = geo.es_beta[t];
+        for (int l = 0; l < W; ++l) {
+          const double y = c - (double)l, z = 1.0 - (y * y) * geo.es_ia2;
+          const double s = z > 0.0 ? sqrt(z) : 0.0;
+          const double e = z > 0.0 ? exp(beta * (s - 1.0)) : 0.0;
+          w[t][l] = (T)e;
+          dw[t][l] = z > 0.0 ? (T)(-e * beta * y * geo.es_ia2 / s * (double)geo.n[t]) : (T)0;
+        }
+      } else {
+        const double ib = 1.0 / geo.b[t];
+        for (int l = 0; l < W; ++l) {
+          const double y = c - (double)l;
+          const double e = exp(-(y * y) * ib);
+          w[t][l] = (T)e;
+          dw[t][l] = (T)(-2.0 * y * ib * e * (double)geo.n[t]);
+        }
       }
     }
     for (int t = d; t < kMaxDim; ++t) {

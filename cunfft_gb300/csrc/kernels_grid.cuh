@@ -43,13 +43,16 @@ __host__ __device__ constexpr int off_bits(int d) { return d == 1 ? 30 : (d == 2
 template <typename T> struct WeightMath;
 
 template <> struct WeightMath<float> {
-  // psi(l) / sqrt(b') = exp(-(fr + m - l)^2 / b) = exp2(-(y*y) * log2(e)/b)
+  // Gaussian: psi(l) / sqrt(b') = exp(-(fr + m - l)^2 / b) = exp2(-(y*y) * log2(e)/b);
+  // ES: exp(beta (sqrt(1 - y^2/alpha^2) - 1)), y = fr + m - l
   static __device__ __forceinline__ void taps(float fr, int m, const Geom& g, int t, int W, float* out) {
-    const float cb = t == 0 ? g.cbf[0] : (t == 1 ? g.cbf[1] : g.cbf[2]);
+    const TapK k = tap_k(g, t);
+    if (g.window == kWinES) {
 #pragma unroll 4
-    for (int l = 0; l < W; ++l) {
-      const float y = fr + (float)(m - l);
-      out[l] = exp2f(-(y * y) * cb);
+      for (int l = 0; l < W; ++l) out[l] = win_tap<kWinES>(fr + (float)(m - l), k);
+    } else {
+#pragma unroll 4
+      for (int l = 0; l < W; ++l) out[l] = win_tap<kWinGauss>(fr + (float)(m - l), k);
     }
   }
 };
@@ -57,6 +60,15 @@ template <> struct WeightMath<float> {
 template <> struct WeightMath<double> {
   // FGG form: psi_l = phi * E^l * exp(-l^2/b), phi = exp(-c^2/b), E = exp(2c/b), c = m + fr.
   static __device__ __forceinline__ void taps(double fr, int m, const Geom& g, int t, int W, double* out) {
+    if (g.window == kWinES) {  // exp(beta (sqrt(1 - y^2/alpha^2) - 1)), zero outside |y| < alpha
+      const double beta = t == 0 ? g.es_beta[0] : (t == 1 ? g.es_beta[1] : g.es_beta[2]);
+      const double c = (double)m + fr;
+      for (int l = 0; l < W; ++l) {
+        const double y = c - (double)l, z = 1.0 - (y * y) * g.es_ia2;
+        out[l] = z > 0.0 ? exp(beta * (sqrt(z) - 1.0)) : 0.0;
+      }
+      return;
+    }
     const double b = t == 0 ? g.b[0] : (t == 1 ? g.b[1] : g.b[2]);
     const double c = (double)m + fr;
     const double ib = 1.0 / b;

@@ -113,7 +113,7 @@ __device__ __forceinline__ ItRec it_load_rec(const ItCursor& c, int num_items, i
   return r;
 }
 
-template <int W>
+template <int W, int WIN>
 __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const float2* __restrict__ g, float2* __restrict__ f,
                                                              Geom geo, Tiling tl, Bins bins) {
   constexpr int E1 = it_e1(W), CH = it_ch(W), NCOL = it_ncol(W), N = it_n(W);
@@ -279,7 +279,7 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const float2* __res
     const int slot = 32 * q + lane;     // node slot in the batch = TMEM lane = A row
     const float norm = (float)geo.norm;
     const float mf = (float)geo.m;
-    const float cb0 = geo.cbf[0], cb1 = geo.cbf[1], cb2 = geo.cbf[2];
+    const TapK k0 = tap_k<WIN>(geo, 0), k1 = tap_k<WIN>(geo, 1), k2 = tap_k<WIN>(geo, 2);
     auto build_a = [&](const ItRec& r, uint32_t ab) {
       unsigned char* ah = smem + L.a_off + ab * 2u * L.a_bytes;
       unsigned char* al = ah + L.a_bytes;
@@ -287,10 +287,10 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const float2* __res
 #pragma unroll
       for (int k4 = 0; k4 < kItK / 4; ++k4) {
         float4 v;
-        v.x = tc_tap(r.fr2, mf, 4 * k4 + 0 - o2, W, cb2);
-        v.y = tc_tap(r.fr2, mf, 4 * k4 + 1 - o2, W, cb2);
-        v.z = tc_tap(r.fr2, mf, 4 * k4 + 2 - o2, W, cb2);
-        v.w = tc_tap(r.fr2, mf, 4 * k4 + 3 - o2, W, cb2);
+        v.x = tc_tap<WIN>(r.fr2, mf, 4 * k4 + 0 - o2, W, k2);
+        v.y = tc_tap<WIN>(r.fr2, mf, 4 * k4 + 1 - o2, W, k2);
+        v.z = tc_tap<WIN>(r.fr2, mf, 4 * k4 + 2 - o2, W, k2);
+        v.w = tc_tap<WIN>(r.fr2, mf, 4 * k4 + 3 - o2, W, k2);
         float4 h, l;
         tc_split4(v, h, l);
         const uint32_t oa = (uint32_t)(slot >> 3) * kItSBOA + (uint32_t)k4 * kItLBO + (uint32_t)(slot & 7) * 16u;
@@ -316,9 +316,9 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const float2* __res
       // expanded w0 (planes) and w1 (rows) of this node
       float w0x[E0MAX], w1x[E1];
 #pragma unroll
-      for (int p = 0; p < E0MAX; ++p) w0x[p] = tc_tap(rc.fr0, mf, p - o0, W, cb0);
+      for (int p = 0; p < E0MAX; ++p) w0x[p] = tc_tap<WIN>(rc.fr0, mf, p - o0, W, k0);
 #pragma unroll
-      for (int p = 0; p < E1; ++p) w1x[p] = tc_tap(rc.fr1, mf, p - o1, W, cb1);
+      for (int p = 0; p < E1; ++p) w1x[p] = tc_tap<WIN>(rc.fr1, mf, p - o1, W, k1);
       float accx = 0.f, accy = 0.f;
 #pragma unroll
       for (int c = 0; c < MAXCH; ++c) {

@@ -81,7 +81,8 @@ __global__ void __launch_bounds__(spread_reg_threads_max<W>()) k_spread_reg(cons
   const float norm = (float)geo.norm;
   // staging role: (node sq, dim st) for the weights, node threadIdx.x for the record
   const int sq = threadIdx.x / 3, st = threadIdx.x - sq * 3;
-  const float cbs = st == 0 ? geo.cbf[0] : (st == 1 ? geo.cbf[1] : geo.cbf[2]);
+  const TapK tks = tap_k(geo, st);
+  const bool es = geo.window == kWinES;
   const float mf = (float)geo.m;
 
   while (next_item(bins, 1, &cur)) {
@@ -105,15 +106,21 @@ __global__ void __launch_bounds__(spread_reg_threads_max<W>()) k_spread_reg(cons
       const int nb = min(kRegBatch, item.z - bs);
       RegNode<W>* sb = stage + buf * kRegBatch;
       if (sq < nb) {
-        // tap l of dim st: exp(-(fr + m - l)^2 / b_st), as WeightMath<float>::taps
+        // tap l of dim st at y = fr + m - l, as WeightMath<float>::taps
         RegNode<W>& nd = sb[sq];
+        float wt[W];
+        if (es) {
+#pragma unroll
+          for (int l = 0; l < W; ++l) wt[l] = win_tap<kWinES>(pf_fr + (mf - (float)l), tks);
+        } else {
+#pragma unroll
+          for (int l = 0; l < W; ++l) wt[l] = win_tap<kWinGauss>(pf_fr + (mf - (float)l), tks);
+        }
 #pragma unroll
         for (int l = 0; l < W; ++l) {
-          const float y = pf_fr + (mf - (float)l);
-          const float w = exp2f(-(y * y) * cbs);
-          if (st == 0) nd.w0[l] = w;
-          else if (st == 1) nd.w1p[l] = make_float2(w, w);
-          else nd.w2[l] = w;
+          if (st == 0) nd.w0[l] = wt[l];
+          else if (st == 1) nd.w1p[l] = make_float2(wt[l], wt[l]);
+          else nd.w2[l] = wt[l];
         }
       }
       if ((int)threadIdx.x < nb) {

@@ -149,7 +149,7 @@ __global__ void k_permute_samples(const float2* __restrict__ f, const int32_t* _
     fp[k] = f[sidx[k]];
 }
 
-template <int W>
+template <int W, int WIN>
 __global__ void __launch_bounds__(kTcThreads, 1) k_spread_tc(const float2* __restrict__ f, float2* __restrict__ g,
                                                              Geom geo, Tiling tl, Bins bins) {
   constexpr int T1 = fixed_t_mid(3, W), T2 = fixed_t_last(3, W);
@@ -209,7 +209,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spread_tc(const float2* __res
     const float2* fperm = reinterpret_cast<const float2*>(bins.fperm);
     const float norm = (float)geo.norm;
     const float mf = (float)geo.m;
-    const float cb0 = geo.cbf[0], cb1 = geo.cbf[1], cb2 = geo.cbf[2];
+    const TapK k0 = tap_k<WIN>(geo, 0), k1 = tap_k<WIN>(geo, 1), k2 = tap_k<WIN>(geo, 2);
     // this thread's A rows (row groups warp + kTcBuilders i): offsets into wx, -1 past the tile
     int a_off0[kAIters], a_off1[kAIters];
 #pragma unroll
@@ -278,7 +278,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spread_tc(const float2* __res
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
           const int j = kg * 4 + u;
-          const float w2 = tc_tap(frac[j * 3 + 2], mf, p2 - (int)(roff[j] >> (2 * SH)), W, cb2);
+          const float w2 = tc_tap<WIN>(frac[j * 3 + 2], mf, p2 - (int)(roff[j] >> (2 * SH)), W, k2);
           const float2 c = val[j];
           vv[u] = w2 * norm * (part ? c.y : c.x);
         }
@@ -291,8 +291,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spread_tc(const float2* __res
         for (int i = tid - (kTcN / 8) * 32; i < (E0 + E1) * kTcK; i += kExpWarps * 32) {
           const int j = i & (kTcK - 1), p = i / kTcK;
           const uint32_t off = roff[j];
-          wx[p * kTcWxStride + j] = p < E0 ? tc_tap(frac[j * 3 + 0], mf, p - (int)(off & MASK), W, cb0)
-                                           : tc_tap(frac[j * 3 + 1], mf, (p - E0) - (int)((off >> SH) & MASK), W, cb1);
+          wx[p * kTcWxStride + j] = p < E0 ? tc_tap<WIN>(frac[j * 3 + 0], mf, p - (int)(off & MASK), W, k0)
+                                           : tc_tap<WIN>(frac[j * 3 + 1], mf, (p - E0) - (int)((off >> SH) & MASK), W, k1);
         }
       }
       cp_async_wait_group<kTcAhead - 1>();  // this thread's loads of batch gb + 1 have landed

@@ -207,6 +207,101 @@ int plan_set_spread_kernel(Plan* p, int kind) {
   return set_status(p, CUNFFT_X_SUCCESS, nullptr);
 }
 
+// Gauss-Legendre nodes and weights on [-1, 1]: roots of P_q by Newton's method
+// from the asymptotic guess cos(pi (i + 3/4) / (q + 1/2)), P_q and P_q' by the
+// three-term recurrence, weights 2 / ((1 - z^2) P_q'(z)^2).
+static void gauss_legendre(int q, std::vector<double>& x, std::vector<double>& w) {
+  x.assign(q, 0.0);
+  w.assign(q, 0.0);
+  for (int i = 0; i < (q + 1) / 2; ++i) {
+    double z = cos(M_PI * (i + 0.75) / (q + 0.5)), p0 = 1.0, p1 = 0.0;
+    for (int it = 0; it < 100; ++it) {
+      p0 = 1.0;
+      p1 = 0.0;
+      for (int j = 1; j <= q; ++j) {
+        const double p2 = p1;
+        p1 = p0;
+        p0 = ((2.0 * j - 1.0) * z * p1 - (j - 1.0) * p2) / j;
+      }
+      const double dz = p0 / (q * (z * p0 - p1) / (z * z - 1.0));
+      z -= dz;
+      if (fabs(dz) < 1e-15) break;
+    }
+    p0 = 1.0;
+    p1 = 0.0;
+    for (int j = 1; j <= q; ++j) {
+      const double p2 = p1;
+      p1 = p0;
+      p0 = ((2.0 * j - 1.0) * z * p1 - (j - 1.0) * p2) / j;
+    }
+    const double dp = q * (z * p0 - p1) / (z * z - 1.0);
+    x[i] = -z;
+    x[q - 1 - i] = z;
+    w[i] = w[q - 1 - i] = 2.0 / ((1.0 - z * z) * dp * dp);
+  }
+}
+
+// Window constants of every dimension.  ES: support alpha = m + 1/2 (every grid
+// point closer than alpha to the node is one of the 2m+2 taps of the window-start
+// rule), beta_t = 0.97 pi (2 alpha)(1 - 1/(2 sigma_t)) (Barnett, Magland and
+// af Klinteberg, SIAM J. Sci. Comput. 41 (2019)); the scaling sits in the roll-off
+// factors, so norm = 1.
+static void window_constants(Geom& g, int window) {
+  g.window = window;
+  const double alpha = g.m + 0.5;
+  g.es_ia2 = 1.0 / (alpha * alpha);
+  g.es_ia2f = (float)g.es_ia2;
+  g.norm = 1.0;
+  for (int t = 0; t < kMaxDim; ++t) {
+    g.es_beta[t] = 0.0;
+    g.es_bl[t] = 0.f;
+  }
+  for (int t = 0; t < g.d; ++t) {
+    const double sigma = (double)g.n[t] / (double)g.N[t];
+    if (window == kWinES) {
+      g.es_beta[t] = 0.97 * M_PI * (2.0 * alpha) * (1.0 - 1.0 / (2.0 * sigma));
+      g.es_bl[t] = (float)(g.es_beta[t] * 1.4426950408889634);
+    } else {
+      g.norm *= sqrt((2.0 * sigma - 1.0) / (2.0 * sigma * (double)g.m));
+    }
+  }
+}
+
+// Per-dimension roll-off factors 1 / phi_hat_t(k / n_t) for k in I_N, the
+// dimension's table at offset sum_{s<t} N_s.  Gaussian: exp(fac_t k^2), fac_t =
+// pi^2 b_t / n_t^2 (src/cunfft.cu:87; the constant 1/sqrt(pi b) is the kernels'
+// norm).  ES: phi_hat(xi) = 2 int_0^alpha phi(y) cos(2 pi xi y) dy by 64-point
+// Gauss-Legendre quadrature.
+static std::vector<double> roc_factors(const Geom& g) {
+  std::vector<double> tab;
+  std::vector<double> gx, gw;
+  if (g.window == kWinES) gauss_legendre(64, gx, gw);
+  const double alpha = g.m + 0.5;
+  for (int t = 0; t < g.d; ++t) {
+    if (g.window == kWinES) {
+      std::vector<double> yq(gx.size()), wq(gx.size());
+      for (size_t i = 0; i < gx.size(); ++i) {
+        yq[i] = 0.5 * alpha * (gx[i] + 1.0);
+        const double z = 1.0 - yq[i] * yq[i] * g.es_ia2;
+        wq[i] = alpha * gw[i] * exp(g.es_beta[t] * (sqrt(z > 0.0 ? z : 0.0) - 1.0));  // 2 x (alpha / 2) x w_i x phi
+      }
+      for (int64_t c = 0; c < g.N[t]; ++c) {
+        const double xi = (double)(c - g.N[t] / 2) / (double)g.n[t];
+        double ph = 0.0;
+        for (size_t i = 0; i < yq.size(); ++i) ph += wq[i] * cos(2.0 * M_PI * xi * yq[i]);
+        tab.push_back(1.0 / ph);
+      }
+    } else {
+      const double fac = (M_PI * M_PI * g.b[t]) / (double)(g.n[t] * g.n[t]);
+      for (int64_t c = 0; c < g.N[t]; ++c) {
+        const double k = (double)(c - g.N[t] / 2);
+        tab.push_back(exp(fac * k * k));
+      }
+    }
+  }
+  return tab;
+}
+
 // Geometry of a plan (parameters, window constants, device attributes); no
 // device or host allocation.
 int geom_init(Plan* p, int d, const int64_t* N, const int64_t* n, int m, int prec, int batch) {
@@ -241,16 +336,34 @@ int geom_init(Plan* p, int d, const int64_t* N, const int64_t* n, int m, int pre
     const double sigma = (double)nt / (double)N[t];
     g.b[t] = (2.0 * sigma) / (2.0 * sigma - 1.0) * ((double)m / M_PI);
     g.cbf[t] = (float)(1.4426950408889634 / g.b[t]);
-    g.norm *= sqrt((2.0 * sigma - 1.0) / (2.0 * sigma * (double)m));
     g.Ntot *= N[t];
     g.ntot *= nt;
   }
   if (g.ntot * batch >= ((int64_t)1 << 40)) return set_status(p, CUNFFT_X_INVALID_ARGUMENT, "grid too large");
+  window_constants(g, kWinGauss);
   p->prec = prec;
   CG_TRY(check_cuda(p, cudaGetDevice(&p->device), "cudaGetDevice"));
   CG_TRY(check_cuda(p, cudaDeviceGetAttribute(&p->num_sms, cudaDevAttrMultiProcessorCount, p->device),
                     "cudaDeviceGetAttribute"));
   return CUNFFT_X_SUCCESS;
+}
+
+int plan_window(const Plan* p) { return p->geo.window; }
+
+// Switch the window: new tap constants and roll-off factors (same table size);
+// captured graphs hold the old constants by value and are re-captured.
+int plan_set_window(Plan* p, int window) {
+  if (window != kWinGauss && window != kWinES)
+    return set_status(p, CUNFFT_X_INVALID_ARGUMENT, "unknown window %d", window);
+  if (window != p->geo.window) {
+    CG_TRY(check_cuda(p, cudaStreamSynchronize(p->stream), "cudaStreamSynchronize"));  // the old table may be in use
+    window_constants(p->geo, window);
+    const std::vector<double> tab = roc_factors(p->geo);
+    CG_TRY(check_cuda(p, cudaMemcpy(p->roc_tab, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice),
+                      "upload roll-off table"));
+    ++p->node_gen;
+  }
+  return set_status(p, CUNFFT_X_SUCCESS, nullptr);
 }
 
 int plan_init(Plan* p, int d, const int64_t* N, const int64_t* n, int m, int prec, int batch, cudaStream_t stream,
@@ -266,16 +379,9 @@ int plan_init(Plan* p, int d, const int64_t* N, const int64_t* n, int m, int pre
   }
   for (int i = 0; i < 8; ++i) CG_TRY(check_cuda(p, cudaEventCreate(&p->ev[i]), "cudaEventCreate"));
   p->timing = true;
-  // roll-off factor tables exp(fac_t k_t^2), fac_t = pi^2 b_t / n_t^2 (src/cunfft.cu:87)
+  // roll-off factor tables, per dimension
   {
-    std::vector<double> tab;
-    for (int t = 0; t < d; ++t) {
-      const double fac = (M_PI * M_PI * g.b[t]) / (double)(g.n[t] * g.n[t]);
-      for (int64_t c = 0; c < g.N[t]; ++c) {
-        const double k = (double)(c - g.N[t] / 2);
-        tab.push_back(exp(fac * k * k));
-      }
-    }
+    const std::vector<double> tab = roc_factors(g);
     CG_TRY(check_cuda(p, cudaMalloc(&p->roc_tab, sizeof(double) * tab.size()), "cudaMalloc roll-off table"));
     CG_TRY(check_cuda(p, cudaMemcpy(p->roc_tab, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice),
                       "upload roll-off table"));

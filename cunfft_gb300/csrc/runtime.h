@@ -33,7 +33,7 @@ struct Plan {
   cufftHandle fft_bwd_ext = 0;
   void* g = nullptr;           // batch * ntot complex
   bool own_g = false;
-  double* roc_tab = nullptr;   // per-dim roll-off factors exp(fac_t k_t^2), sum_t N_t doubles
+  double* roc_tab = nullptr;   // per-dim roll-off factors 1 / phi_hat_t(k_t / n_t), sum_t N_t doubles
   Tiling tl{};
   Bins bins{};
   int64_t bins_capacity_M = -1;
@@ -64,6 +64,9 @@ struct Plan {
 };
 
 inline size_t plan_elem_bytes(const Plan* p) { return p->prec == kF64 ? 16 : 8; }
+
+int plan_window(const Plan* p);
+int plan_set_window(Plan* p, int window);
 
 // return the status of a runtime call when it is not CUNFFT_X_SUCCESS
 #define CG_TRY(expr)                          \

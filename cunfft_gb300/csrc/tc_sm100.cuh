@@ -12,6 +12,8 @@
 
 #include <stdint.h>
 
+#include "common.cuh"
+
 namespace cg {
 namespace tc {
 
@@ -165,13 +167,12 @@ __device__ __forceinline__ void tc_split4(float4 v, float4& hi, float4& lo) {
   lo.w = v.w - hi.w;
 }
 
-// Gaussian tap exp(-(fr + m - l)^2 / b) = exp2(-(fr + m - l)^2 cb), the FP32 tap of
-// WeightMath<float>::taps (cb = log2(e) / b), zero outside the window 0 <= l < W.
-// The exponential is evaluated for every l and then selected: lanes hold different
-// windows, and a branch around it would diverge on every tap.
-__device__ __forceinline__ float tc_tap(float fr, float mf, int l, int W, float cb) {
-  const float y = fr + (mf - (float)l);
-  const float e = exp2f(-(y * y) * cb);
+// Window tap at y = fr + m - l, the FP32 tap of WeightMath<float>::taps, zero outside
+// the window 0 <= l < W.  The tap is evaluated for every l and then selected: lanes
+// hold different windows, and a branch around it would diverge on every tap.
+template <int WIN>
+__device__ __forceinline__ float tc_tap(float fr, float mf, int l, int W, TapK k) {
+  const float e = win_tap<WIN>(fr + (mf - (float)l), k);
   return (unsigned)l < (unsigned)W ? e : 0.f;
 }
 

@@ -141,6 +141,17 @@ int cunfft_x_get_spread_kernel(const cunfft_x_plan* h, int* kind) {
   return CUNFFT_X_SUCCESS;
 }
 
+int cunfft_x_set_window(cunfft_x_plan* h, int window) {
+  if (!h) return CUNFFT_X_INVALID_ARGUMENT;
+  return cg::plan_set_window(&h->p, window);
+}
+
+int cunfft_x_get_window(const cunfft_x_plan* h, int* window) {
+  if (!h || !window) return CUNFFT_X_INVALID_ARGUMENT;
+  *window = cg::plan_window(&h->p);
+  return CUNFFT_X_SUCCESS;
+}
+
 int cunfft_x_forward_host(cunfft_x_plan* h, const double* x_host, const int64_t* M, const void* fhat_host,
                           void* f_host) {
   if (!h) return CUNFFT_X_INVALID_ARGUMENT;

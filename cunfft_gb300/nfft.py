@@ -1,6 +1,6 @@
 """Python front end of the extension API (include/cunfft_x.h) for torch CUDA tensors.
 
-``NFFT`` wraps one cunfft_x plan: d-variate Gaussian-window NFFT (d = 1..3) in
+``NFFT`` wraps one cunfft_x plan: d-variate NFFT (d = 1..3, Gaussian or ES window) in
 FP64 (the reference's form) or FP32 (FP32 gridding and FFT, FP64 node
 reduction and roll-off factors), for ``batch`` instances with uneven node
 counts.  Tensors stay on the device; calls run on the plan's CUDA stream, which
@@ -22,7 +22,7 @@ def _ptr(t):
 
 
 class NFFT:
-    def __init__(self, N, n=None, m=6, precision="f64", batch=1, device=None, stream=None):
+    def __init__(self, N, n=None, m=6, precision="f64", batch=1, device=None, stream=None, window="gaussian"):
         self._host_refs = []  # host tensors in flight in host-buffer transforms
         self._lib = nat.lib()
         self.N = [int(v) for v in N]
@@ -52,6 +52,8 @@ class NFFT:
         self.x = None
         self.M_inst = [0] * self.batch
         self.M = 0
+        if window != "gaussian":
+            self.set_window(window)
 
     def _grid_sizes(self, n):
         if n is not None:
@@ -215,6 +217,19 @@ class NFFT:
         nat.check(self._lib.cunfft_x_get_tiling(self._h, T, ctypes.byref(chunk), ctypes.byref(threads)))
         return {"T": list(T)[: self.d], "chunk": chunk.value, "threads": threads.value, "spread": self.spread_kernel(),
                 "interp": self.interp_kernel()}
+
+    WINDOWS = {"gaussian": 0, "es": 1}
+
+    def set_window(self, window):
+        """Gridding window: "gaussian" (the reference's) or "es" (exponential of
+        semicircle, about 1e-12 relative error at m = 6, sigma = 2)."""
+        nat.check(self._lib.cunfft_x_set_window(self._h, self.WINDOWS[window]), self._h)
+        return self
+
+    def window(self):
+        k = ctypes.c_int()
+        nat.check(self._lib.cunfft_x_get_window(self._h, ctypes.byref(k)))
+        return {v: n for n, v in self.WINDOWS.items()}[k.value]
 
     SPREAD_KERNELS = {"auto": 0, "shared": 1, "register": 2, "global": 3, "tensor": 4}
 

@@ -177,6 +177,26 @@ int cunfft_x_set_spread_kernel(cunfft_x_plan *plan, int kind);
 /** Spreading kernel in use: CUNFFT_X_SPREAD_SHARED, _REGISTER, _TENSOR or _GLOBAL. */
 int cunfft_x_get_spread_kernel(const cunfft_x_plan *plan, int *kind);
 
+/** Window of the gridding.  GAUSSIAN is the reference's (src/cunfft.cu:60-87: taps
+ *  exp(-(y^2)/b), b = 2 sigma/(2 sigma - 1) m/pi, roll-off exp(pi^2 b k^2/n^2)).
+ *  ES is the exponential of semicircle exp(beta (sqrt(1 - y^2/alpha^2) - 1)) on
+ *  |y| < alpha = m + 1/2 grid cells, beta = 0.97 pi (2m+1)(1 - 1/(2 sigma))
+ *  (Barnett, Magland, af Klinteberg, SIAM J. Sci. Comput. 41 (2019)), roll-off
+ *  1/phi_hat(k/n) by Gauss-Legendre quadrature.  Same taps per node (2m+2 per
+ *  dimension), same kernels; at sigma = 2 its error falls about tenfold per unit
+ *  of window width: about 1e-12 at m = 6 where the Gaussian stops near 1e-6. */
+enum {
+  CUNFFT_X_WINDOW_GAUSSIAN = 0,
+  CUNFFT_X_WINDOW_ES = 1
+};
+
+/** Select the window (default GAUSSIAN).  Waits for the plan's stream; bound nodes
+ *  stay bound; captured graphs are re-captured on their next launch. */
+int cunfft_x_set_window(cunfft_x_plan *plan, int window);
+
+/** Window in use. */
+int cunfft_x_get_window(const cunfft_x_plan *plan, int *window);
+
 /** Request an interpolation kernel (CUNFFT_X_INTERP_AUTO, _SHARED or _TENSOR);
  *  TENSOR on a plan it does not cover returns CUNFFT_X_UNSUPPORTED.  The request
  *  holds across later tilings (a tiling TENSOR does not cover runs SHARED). */

@@ -23,6 +23,13 @@
  *   - example data          src/cuda_util.cpp:151-171, 204-212 (drand48 order)
  *   - error norm            src/cuda_util.cpp:237-258
  *
+ * A second window, not in the reference, checks the extension API's ES option:
+ * exponential of semicircle phi(y) = exp(beta (sqrt(1 - y^2/alpha^2) - 1)) on
+ * |y| < alpha = m + 1/2, beta = 0.97 pi (2m+1)(1 - 1/(2 sigma)) (Barnett, Magland,
+ * af Klinteberg, SIAM J. Sci. Comput. 41 (2019)), roll-off 1/phi_hat(k/n) with
+ * phi_hat by composite Simpson quadrature (orc_set_window(1)).  Its accuracy is
+ * pinned against the direct NDFT, not against the reference.
+ *
  * Parity is pinned against the E_inf known answers of the reference's own
  * result logs (Tests/Runtime/*.txt), which the reference produced from
  * drand48's default state; see tests/golden/.
@@ -138,7 +145,14 @@ static void node_weights(double c, double sigma, double b, int m, const double *
     }
 }
 
+/* Window of the restated method: 0 the reference's Gaussian, 1 ES (see above). */
+static int orc_win = 0;
+void orc_set_window(int w) { orc_win = w; }
+int orc_get_window(void) { return orc_win; }
+
 typedef struct {
+    int win;
+    double es_beta[ORC_MAXD];
     int d, m, W;
     int64_t N[ORC_MAXD], n[ORC_MAXD];
     int64_t Ntot, ntot;
@@ -157,7 +171,37 @@ static int plan_setup(oplan *p, int d, const int64_t *N, const int64_t *n, int m
     }
     orc_params(d, N, n, m, p->sigma, p->b, p->fac);
     for (int t = 0; t < d; ++t) orc_fg_exp_l(p->fg[t], p->b[t], p->W);
+    p->win = orc_win;
+    for (int t = 0; t < d; ++t)
+        p->es_beta[t] = 0.97 * M_PI * (2.0 * m + 1.0) * (1.0 - 1.0 / (2.0 * p->sigma[t]));
     return 0;
+}
+
+static double es_phi(double y, double beta, double alpha)
+{
+    double z = 1.0 - (y / alpha) * (y / alpha);
+    return z > 0.0 ? exp(beta * (sqrt(z) - 1.0)) : 0.0;
+}
+
+/* 1 / phi_hat_t(k / n_t) for k = c - N_t/2, c = 0..N_t-1: phi_hat(xi) =
+ * 2 int_0^alpha phi(y) cos(2 pi xi y) dy, composite Simpson on 40000 intervals. */
+static double *es_roc_table(const oplan *p, int t)
+{
+    const int K = 40000;
+    const double alpha = p->m + 0.5, h = alpha / K;
+    double *ph = (double *)malloc(sizeof(double) * (K + 1));
+    double *tab = (double *)malloc(sizeof(double) * (size_t)p->N[t]);
+    for (int i = 0; i <= K; ++i) {
+        double sw = (i == 0 || i == K) ? 1.0 : ((i % 2) ? 4.0 : 2.0);
+        ph[i] = sw * es_phi(i * h, p->es_beta[t], alpha);
+    }
+    for (int64_t c = 0; c < p->N[t]; ++c) {
+        double xi = (double)(c - p->N[t] / 2) / (double)p->n[t], acc = 0.0;
+        for (int i = 0; i <= K; ++i) acc += ph[i] * cos(2.0 * M_PI * xi * (i * h));
+        tab[c] = 1.0 / (2.0 * acc * h / 3.0);
+    }
+    free(ph);
+    return tab;
 }
 
 /* Node -> (u_t, weights) for all dims. */
@@ -166,7 +210,11 @@ static void node_setup(const oplan *p, const double *xj, int64_t *u, double w[][
     for (int t = 0; t < p->d; ++t) {
         u[t] = orc_window_start(xj[t], p->n[t], p->m);
         double c = (double)p->n[t] * xj[t] - (double)u[t];
-        node_weights(c, p->sigma[t], p->b[t], p->m, p->fg[t], p->W, w[t]);
+        if (p->win == 1) {
+            for (int l = 0; l < p->W; ++l) w[t][l] = es_phi(c - (double)l, p->es_beta[t], p->m + 0.5);
+        } else {
+            node_weights(c, p->sigma[t], p->b[t], p->m, p->fg[t], p->W, w[t]);
+        }
     }
 }
 
@@ -195,22 +243,34 @@ static double roc_factor(const oplan *p, const int64_t *k)
     return exp(s);
 }
 
-/* g = 0 outside I_N; g[k mod n] = fhat[k] * exp(sum fac k^2). */
+static double es_roc_factor(const oplan *p, double *const *tab, const int64_t *k)
+{
+    double f = 1.0;
+    for (int t = 0; t < p->d; ++t) f *= tab[t][k[t] + p->N[t] / 2];
+    return f;
+}
+
+/* g = 0 outside I_N; g[k mod n] = fhat[k] * exp(sum fac k^2) (Gaussian), or
+ * fhat[k] * prod_t 1/phi_hat_t(k_t/n_t) (ES). */
 void orc_roc_forward(int d, const int64_t *N, const int64_t *n, int m,
                      const double *fhat, double *g)
 {
     oplan p;
     if (plan_setup(&p, d, N, n, m)) return;
+    double *es_tab[ORC_MAXD] = {NULL, NULL, NULL};
+    if (p.win == 1)
+        for (int t = 0; t < d; ++t) es_tab[t] = es_roc_table(&p, t);
     memset(g, 0, sizeof(double) * 2 * (size_t)p.ntot);
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < p.Ntot; ++i) {
         int64_t k[ORC_MAXD];
         coef_index_to_k(&p, i, k);
         int64_t gi = grid_index_of_k(&p, k);
-        double f = roc_factor(&p, k);
+        double f = p.win == 1 ? es_roc_factor(&p, es_tab, k) : roc_factor(&p, k);
         g[2 * gi] = fhat[2 * i] * f;
         g[2 * gi + 1] = fhat[2 * i + 1] * f;
     }
+    for (int t = 0; t < d; ++t) free(es_tab[t]);
 }
 
 /* fhat[k] = g[k mod n] * exp(sum fac k^2). */
@@ -219,15 +279,19 @@ void orc_roc_adjoint(int d, const int64_t *N, const int64_t *n, int m,
 {
     oplan p;
     if (plan_setup(&p, d, N, n, m)) return;
+    double *es_tab[ORC_MAXD] = {NULL, NULL, NULL};
+    if (p.win == 1)
+        for (int t = 0; t < d; ++t) es_tab[t] = es_roc_table(&p, t);
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < p.Ntot; ++i) {
         int64_t k[ORC_MAXD];
         coef_index_to_k(&p, i, k);
         int64_t gi = grid_index_of_k(&p, k);
-        double f = roc_factor(&p, k);
+        double f = p.win == 1 ? es_roc_factor(&p, es_tab, k) : roc_factor(&p, k);
         fhat[2 * i] = g[2 * gi] * f;
         fhat[2 * i + 1] = g[2 * gi + 1] * f;
     }
+    for (int t = 0; t < d; ++t) free(es_tab[t]);
 }
 
 /* ------------------------------------------------------------------------ */

@@ -45,8 +45,27 @@ def lib():
         L.orc_error_l_infty.restype = ctypes.c_double
         L.orc_error_l_infty.argtypes = [_pd, _pd, _i64]
         L.orc_num_threads.restype = ctypes.c_int
+        L.orc_set_window.argtypes = [ctypes.c_int]
+        L.orc_get_window.restype = ctypes.c_int
         _lib = L
     return _lib
+
+
+WINDOWS = {"gaussian": 0, "es": 1}
+
+
+class _window:
+    """Select the restated method's window for one call (the reference's Gaussian
+    otherwise); the C oracle keeps it in a global."""
+
+    def __init__(self, window):
+        self.w = WINDOWS[window]
+
+    def __enter__(self):
+        lib().orc_set_window(self.w)
+
+    def __exit__(self, *exc):
+        lib().orc_set_window(0)
 
 
 def _dp(a):
@@ -120,19 +139,21 @@ def _r(a):
     return np.ascontiguousarray(a, dtype=np.float64)
 
 
-def roc_forward(fhat, N, n, m):
+def roc_forward(fhat, N, n, m, window="gaussian"):
     N, n = _dims(N), _dims(n)
     fh = _c(fhat).reshape(-1)
     g = np.zeros(int(np.prod(n)), dtype=np.complex128)
-    lib().orc_roc_forward(len(N), _ip(N), _ip(n), m, _dp(fh.view(np.float64)), _dp(g.view(np.float64)))
+    with _window(window):
+        lib().orc_roc_forward(len(N), _ip(N), _ip(n), m, _dp(fh.view(np.float64)), _dp(g.view(np.float64)))
     return g.reshape(tuple(n))
 
 
-def roc_adjoint(g, N, n, m):
+def roc_adjoint(g, N, n, m, window="gaussian"):
     N, n = _dims(N), _dims(n)
     gg = _c(g).reshape(-1)
     fh = np.zeros(int(np.prod(N)), dtype=np.complex128)
-    lib().orc_roc_adjoint(len(N), _ip(N), _ip(n), m, _dp(gg.view(np.float64)), _dp(fh.view(np.float64)))
+    with _window(window):
+        lib().orc_roc_adjoint(len(N), _ip(N), _ip(n), m, _dp(gg.view(np.float64)), _dp(fh.view(np.float64)))
     return fh.reshape(tuple(N))
 
 
@@ -143,44 +164,48 @@ def fft(a, sign):
     return a
 
 
-def interp(x, g, N, n, m):
+def interp(x, g, N, n, m, window="gaussian"):
     N, n = _dims(N), _dims(n)
     x = _r(x).reshape(-1, len(N))
     gg = _c(g).reshape(-1)
     f = np.zeros(x.shape[0], dtype=np.complex128)
-    lib().orc_interp(len(N), _ip(N), _ip(n), m, x.shape[0], _dp(x), _dp(gg.view(np.float64)),
+    with _window(window):
+        lib().orc_interp(len(N), _ip(N), _ip(n), m, x.shape[0], _dp(x), _dp(gg.view(np.float64)),
                      _dp(f.view(np.float64)))
     return f
 
 
-def spread(x, f, N, n, m):
+def spread(x, f, N, n, m, window="gaussian"):
     N, n = _dims(N), _dims(n)
     x = _r(x).reshape(-1, len(N))
     ff = _c(f).reshape(-1)
     g = np.zeros(int(np.prod(n)), dtype=np.complex128)
-    lib().orc_spread(len(N), _ip(N), _ip(n), m, x.shape[0], _dp(x), _dp(ff.view(np.float64)),
+    with _window(window):
+        lib().orc_spread(len(N), _ip(N), _ip(n), m, x.shape[0], _dp(x), _dp(ff.view(np.float64)),
                      _dp(g.view(np.float64)))
     return g.reshape(tuple(n))
 
 
-def nfft_forward(x, fhat, N, n=None, m=6):
+def nfft_forward(x, fhat, N, n=None, m=6, window="gaussian"):
     N = _dims(N)
     n = _dims(default_n(N) if n is None else n)
     x = _r(x).reshape(-1, len(N))
     fh = _c(fhat).reshape(-1)
     f = np.zeros(x.shape[0], dtype=np.complex128)
-    lib().orc_nfft_forward(len(N), _ip(N), _ip(n), m, x.shape[0], _dp(x),
+    with _window(window):
+        lib().orc_nfft_forward(len(N), _ip(N), _ip(n), m, x.shape[0], _dp(x),
                            _dp(fh.view(np.float64)), _dp(f.view(np.float64)))
     return f
 
 
-def nfft_adjoint(x, f, N, n=None, m=6):
+def nfft_adjoint(x, f, N, n=None, m=6, window="gaussian"):
     N = _dims(N)
     n = _dims(default_n(N) if n is None else n)
     x = _r(x).reshape(-1, len(N))
     ff = _c(f).reshape(-1)
     fh = np.zeros(int(np.prod(N)), dtype=np.complex128)
-    lib().orc_nfft_adjoint(len(N), _ip(N), _ip(n), m, x.shape[0], _dp(x),
+    with _window(window):
+        lib().orc_nfft_adjoint(len(N), _ip(N), _ip(n), m, x.shape[0], _dp(x),
                            _dp(ff.view(np.float64)), _dp(fh.view(np.float64)))
     return fh.reshape(tuple(int(v) for v in N))
 

@@ -155,3 +155,24 @@ def test_oracle_general_grid_sizes(N, n):
     lhs = np.vdot(f, O.nfft_forward(x, fh, N, n=n))
     rhs = np.vdot(O.nfft_adjoint(x, f, N, n=n), fh)
     assert abs(lhs - rhs) < 1e-10 * abs(lhs)
+
+
+@pytest.mark.parametrize("N,m,tol", [([64], 6, 1e-10), ([16, 24], 6, 1e-10), ([8, 10, 12], 6, 1e-10),
+                                     ([32], 4, 1e-6), ([16, 16], 8, 1e-12)])
+def test_oracle_es_window_against_ndft(N, m, tol):
+    """The ES window (exponential of semicircle, roll-off by quadrature) is pinned to
+    the direct NDFT: about 1e-12 at m = 6, sigma = 2, where the reference's Gaussian
+    stops near 1e-6; the pair stays adjoint."""
+    rng = np.random.default_rng(m + len(N))
+    M = 120
+    x = rng.uniform(-0.5, 0.5, (M, len(N)))
+    fh = rng.standard_normal(N) + 1j * rng.standard_normal(N)
+    f = rng.standard_normal(M) + 1j * rng.standard_normal(M)
+    fw = O.nfft_forward(x, fh, N, m=m, window="es")
+    ad = O.nfft_adjoint(x, f, N, m=m, window="es")
+    assert O.rel_l2(O.ndft_forward(x, fh, N), fw) < tol
+    assert O.rel_l2(O.ndft_adjoint(x, f, N), ad) < tol
+    assert abs(np.vdot(f, fw) - np.vdot(ad, fh)) < 1e-10 * abs(np.vdot(f, fw))
+    # the window selection does not leak into later Gaussian calls
+    assert O.lib().orc_get_window() == 0
+    assert O.rel_l2(O.ndft_forward(x, fh, N), O.nfft_forward(x, fh, N, m=m)) > 10 * tol
