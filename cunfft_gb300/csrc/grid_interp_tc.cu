@@ -1,4 +1,9 @@
-// grid_interp_tc.cu -- launcher of the tensor-core 3D FP32 interpolation kernel.
+// grid_interp_tc.cu -- launcher of the tensor-core 3D FP32 interpolation: the split of
+// the grid into padded TF32 hi/lo planes, then the TMA-fed kernel.
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+
 #include "kernels_interp_tc.cuh"
 
 namespace cg {
@@ -7,13 +12,71 @@ bool interp_tc_supported(const Plan& p) {
   return p.prec == kF32 && !p.tl.use_global && interp_tc_ok(p.geo.d, p.geo.W, p.tl.T[0], p.geo.n[2]);
 }
 
+// cuTensorMapEncodeTiled from the driver, through the runtime's entry-point query
+// (no link-time dependency on the driver library).
+static PFN_cuTensorMapEncodeTiled_v12000 encode_tiled() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void* ptr = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(ptr);
+  }
+  return fn;
+}
+
+// Split planes float [batch][4][P0][P1][P2s] and the 5-D map over them (dims P2s, P1,
+// P0, component, instance; box 32 floats x E1 rows x CH planes, 128-byte swizzle,
+// zero fill outside).  Box rows are 128 bytes (32 floats), the innermost box extent
+// the swizzle allows; rows are multiples of 16 bytes (P2s % 4 == 0).
+cudaError_t interp_tc_prepare(Plan& p) {
+  if (p.it_ready) return cudaSuccess;
+  const ItSplit sd = it_split_dims(p.geo);
+  const size_t comp = (size_t)(sd.P0 * sd.P1 * sd.P2s);
+  const size_t bytes = sizeof(float) * 4 * comp * (size_t)p.geo.batch;
+  PFN_cuTensorMapEncodeTiled_v12000 enc = encode_tiled();
+  if (!enc) return cudaErrorNotSupported;
+  if (!p.it_split) {
+    cudaError_t e = cudaMalloc(&p.it_split, bytes);
+    if (e != cudaSuccess) {
+      p.it_split = nullptr;
+      return e;
+    }
+  }
+  const int E1 = it_e1(p.geo.W), CH = it_ch(p.geo.W);
+  const cuuint64_t dims[5] = {(cuuint64_t)sd.P2s, (cuuint64_t)sd.P1, (cuuint64_t)sd.P0, 4u, (cuuint64_t)p.geo.batch};
+  const cuuint64_t strides[4] = {(cuuint64_t)(sd.P2s * 4), (cuuint64_t)(sd.P2s * sd.P1 * 4),
+                                 (cuuint64_t)(comp * 4), (cuuint64_t)(4 * comp * 4)};
+  const cuuint32_t box[5] = {(cuuint32_t)kItK, (cuuint32_t)E1, (cuuint32_t)CH, 1u, 1u};
+  const cuuint32_t estr[5] = {1u, 1u, 1u, 1u, 1u};
+  const CUresult r = enc(&p.it_tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 5, p.it_split, dims, strides, box, estr,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
+  p.it_ready = true;
+  return cudaSuccess;
+}
+
+void interp_tc_release(Plan& p) {
+  cudaFree(p.it_split);
+  p.it_split = nullptr;
+  p.it_ready = false;
+}
+
 template <int W>
 static cudaError_t launch_it(const Plan& p, const void* in, void* out, cudaStream_t st) {
-  if (!interp_tc_supported(p)) return cudaErrorInvalidConfiguration;
+  if (!interp_tc_supported(p) || !p.it_ready) return cudaErrorInvalidConfiguration;
+  const ItSplit sd = it_split_dims(p.geo);
+  const int64_t quads = sd.P0 * sd.P1 * (sd.P2s / 4) * p.geo.batch;
+  const int sblocks = (int)std::min<int64_t>((quads + 255) / 256, (int64_t)p.num_sms * 16);
+  k_split_pad<<<sblocks, 256, 0, st>>>((const float2*)in, p.it_split, p.geo, sd);
   // 512 tensor-memory columns per CTA: at most one CTA per SM (more than half the
   // SM's 228 KB of shared memory), so tcgen05.alloc never waits
-  const ItLayout L = it_layout(W);
-  const size_t smem = L.total > 116u * 1024u + 1u ? L.total : 116u * 1024u + 1u;
+  const ItLayout L = it_layout();
+  const size_t smem = L.dyn;
+  static_assert(it_layout().dyn > 116u * 1024u, "one CTA per SM");
   auto kern = p.geo.window == kWinES ? k_interp_tc<W, kWinES> : k_interp_tc<W, kWinGauss>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
@@ -21,7 +84,7 @@ static cudaError_t launch_it(const Plan& p, const void* in, void* out, cudaStrea
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kItThreads, smem);
   if (e != cudaSuccess) return e;
   if (per_sm != 1) return cudaErrorInvalidConfiguration;
-  kern<<<p.num_sms, kItThreads, smem, st>>>((const float2*)in, (float2*)out, p.geo, p.tl, p.bins);
+  kern<<<p.num_sms, kItThreads, smem, st>>>(p.it_tmap, (float2*)out, p.geo, p.tl, p.bins);
   return cudaGetLastError();
 }
 

@@ -1,4 +1,5 @@
-// kernels_interp_tc.cuh -- 3D FP32 interpolation on the tensor cores (tcgen05, 3xTF32).
+// kernels_interp_tc.cuh -- 3D FP32 interpolation on the tensor cores (tcgen05, 3xTF32),
+// tile chunks streamed by TMA.
 //
 // Same work items, tiles and weights as k_interp (kernels_grid.cuh).  For a tile
 // with padded extents E0 x E1 x E2 and a batch of up to 128 of its nodes,
@@ -6,19 +7,26 @@
 //     H[j, (p0, p1, re|im)] = sum_{p2} w2_j[p2 - o2_j] G[(p0, p1), p2] (re|im)
 // and H is the product D = A B^T of
 //     A[j, p2]              = w2_j[p2 - o2_j]                  (128 nodes x 32 columns)
-//     B[(p0, p1, re|im), p2] = Re|Im G[p0, p1, p2]             (the tile, K = p2)
-// computed in chunks of kItCh planes so that a chunk's 2 E1 kItCh columns fit one
-// MMA (N <= 256) and two chunks fit tensor memory.  D lives in tensor memory with
-// node j in lane j, so the thread that owns node j finishes the w0 (x) w1 sum over
-// its window from its own lane, chunk by chunk, in registers.
+//     B[(re|im, p0, p1), p2] = Re|Im G[p0, p1, p2]             (the tile, K = p2)
+// computed in chunks of kItCh planes (the chunk's CH E1 (plane, row) pairs are B rows
+// 0.. of the real part and 128.. of the imaginary part: N = 256), two chunk
+// accumulators in tensor memory.  D lives in tensor memory with node j in lane j, so
+// the thread that owns node j finishes the w0 (x) w1 sum over its window from its own
+// lane, chunk by chunk, in registers.
 //
-// Warp roles: 8 builder warps load the tile chunk by chunk from the grid (L2 / HBM),
-// split it into TF32 hi + lo parts and store it in K-major core-matrix layout
-// (double-buffered); one MMA warp issues hi*hi + hi*lo + lo*hi per k-step of 8
-// columns into one of two tensor-memory buffers; 4 node warps (lane quarters) build
-// A from their nodes' taps and reduce D.  Hand-offs are mbarriers; every wait is
-// bounded and a wait that gives up sets the plan's device status flag.
+// The grid is first split (k_split_pad) into TF32 hi + lo parts of its real and
+// imaginary parts, each a float array over the periodically padded index range
+// [0, n_t + W - 1) per dimension.  Every tile's padded box then lies inside those
+// arrays (no wrap), and one thread loads each chunk with four TMA boxes (hi re, hi im,
+// lo re, lo im; 32 floats x E1 rows x CH planes) straight into the 128-byte swizzled
+// K-major layout the MMAs read.  Warp roles: warp 0 lane 0 issues the TMA loads
+// (two chunk stages), warp 1 lane 0 the MMAs hi*hi + hi*lo + lo*hi per k-step of 8
+// columns, warps 2-5 (lane quarters) build A from their nodes' taps and reduce D.
+// Hand-offs are mbarriers (the chunk stages' with TMA transaction counts); every wait
+// is bounded and a wait that gives up sets the plan's device status flag.
 #pragma once
+
+#include <cuda.h>
 
 #include "kernels_grid.cuh"
 #include "tc_sm100.cuh"
@@ -26,46 +34,77 @@
 namespace cg {
 
 constexpr int kItMaxT0 = 16;       // outer tile extent limit (E0 <= 31 planes)
-constexpr int kItK = 32;           // K: innermost tile columns p2 (E2 <= 31), padded
+constexpr int kItK = 32;           // K: innermost tile columns p2 (E2 <= 31), padded; one 128-byte row
 constexpr int kItNodes = 128;      // nodes per batch (MMA M)
-constexpr int kItBuilders = 8;     // warps loading tile chunks
-constexpr int kItMmaWarp = kItBuilders;
-constexpr int kItNodeWarp0 = kItBuilders + 1;  // 4 node warps: lane quarter = warp % 4
-constexpr int kItThreads = (kItBuilders + 1 + 4) * 32;
-constexpr uint32_t kItLBO = 128;               // core matrices along K
+constexpr int kItTmaWarp = 0;
+constexpr int kItMmaWarp = 1;
+constexpr int kItNodeWarp0 = 2;    // 4 node warps: lane quarter = warp % 4
+constexpr int kItThreads = 6 * 32;
+constexpr uint32_t kItLBO = 128;               // A: core matrices along K
 constexpr uint32_t kItSBOA = 1024;             // A: 8-row groups (32 K values = 8 core matrices)
-constexpr uint32_t kItSBOB = 1040;             // B: 8-row groups, shifted 16 bytes: conflict-free stores
+constexpr uint32_t kItPart = 16384;            // one B part (hi re, hi im, lo re, lo im): 128 rows x 128 bytes
+constexpr uint32_t kItStage = 4 * kItPart;     // one chunk stage: B hi = parts 0-1, B lo = parts 2-3
 constexpr uint32_t kItPolls = 1u << 20;        // mbarrier polls (<= 1 us each) before giving up
 
 __host__ __device__ constexpr int it_e1(int W) { return fixed_t_mid(3, W) + W - 1; }
-__host__ __device__ constexpr int it_ch(int W) { return 256 / (2 * it_e1(W)); }               // planes per chunk
-__host__ __device__ constexpr int it_ncol(int W) { return it_ch(W) * 2 * it_e1(W); }          // used D columns
-__host__ __device__ constexpr int it_n(int W) { return (it_ncol(W) + 15) / 16 * 16; }          // MMA N
-__host__ __device__ constexpr int it_pairs_pad(int W) { return (it_ch(W) * it_e1(W) + 7) / 8 * 8; }
+__host__ __device__ constexpr int it_ch(int W) { return 128 / it_e1(W); }                     // planes per chunk
+__host__ __device__ constexpr int it_pairs(int W) { return it_ch(W) * it_e1(W); }            // (plane, row) pairs <= 128
 
 __host__ __device__ constexpr bool interp_tc_ok(int d, int W, int T0, int64_t n2) {
   return d == 3 && W >= 4 && W <= 16 && T0 >= 1 && T0 <= kItMaxT0 && n2 >= 4 && n2 % 4 == 0;
 }
 
-// Shared-memory layout (byte offsets; host and device agree).
+// Shared-memory layout (byte offsets from a 1024-byte aligned base; host and device agree).
 struct ItLayout {
-  uint32_t a_bytes;    // one A part: 16 row groups
-  uint32_t b_bytes;    // one B part: N / 8 row groups
-  uint32_t a_off;      // 2 buffers x (A hi, A lo)
-  uint32_t b_off;      // 2 buffers x (B hi, B lo)
+  uint32_t b_off;      // 2 chunk stages of kItStage
+  uint32_t a_off;      // 2 buffers x (A hi, A lo), 16 KB each
   uint32_t bar_off;    // afull[2], bfull[2], bempty[2], tfull[2], tempty[2]; tensor-memory base
-  uint32_t total;
+  uint32_t total;      // bytes past the aligned base
+  uint32_t dyn;        // dynamic shared memory to request (alignment slack included)
 };
 
-__host__ __device__ inline ItLayout it_layout(int W) {
-  ItLayout L{};
-  L.a_bytes = 16u * kItSBOA;
-  L.b_bytes = (uint32_t)(it_n(W) / 8) * kItSBOB;
-  L.a_off = 0;
-  L.b_off = 4u * L.a_bytes;
-  L.bar_off = (L.b_off + 4u * L.b_bytes + 15u) & ~15u;
-  L.total = L.bar_off + 96u;
-  return L;
+__host__ __device__ constexpr ItLayout it_layout() {
+  return ItLayout{0u, 2u * kItStage, 2u * kItStage + 4u * 16384u, 2u * kItStage + 4u * 16384u + 96u,
+                  2u * kItStage + 4u * 16384u + 96u + 1024u};
+}
+
+// Padded split planes of the grid: float [batch][4][P0][P1][P2s], component 0 hi re,
+// 1 hi im, 2 lo re, 3 lo im; P_t = n_t + W - 1 holds grid index i mod n_t, P2s = P2
+// rounded up to a multiple of 4 (16-byte rows).
+struct ItSplit {
+  int64_t P0, P1, P2, P2s;
+};
+__host__ __device__ inline ItSplit it_split_dims(const Geom& g) {
+  ItSplit s;
+  s.P0 = g.n[0] + g.W - 1;
+  s.P1 = g.n[1] + g.W - 1;
+  s.P2 = g.n[2] + g.W - 1;
+  s.P2s = (s.P2 + 3) / 4 * 4;
+  return s;
+}
+
+// One thread per 4 consecutive p2 of one padded row: the quad never straddles the grid's
+// wrap (n2 % 4 == 0), reads two float4 of complex data and writes one float4 to each of
+// the four components.
+__global__ void k_split_pad(const float2* __restrict__ g, float* __restrict__ out, Geom geo, ItSplit sd) {
+  const int64_t q4 = sd.P2s / 4, row_q = sd.P1 * q4, per = sd.P0 * row_q, total = per * geo.batch;
+  const int64_t comp = sd.P0 * sd.P1 * sd.P2s;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t inst = e / per, r = e - inst * per;
+    const int64_t i0 = r / row_q, r2 = r - i0 * row_q;
+    const int64_t i1 = r2 / q4, i2 = (r2 - i1 * q4) * 4;
+    const float2* src = g + inst * geo.ntot +
+                        (wrap_up(i0, geo.n[0]) * geo.n[1] + wrap_up(i1, geo.n[1])) * geo.n[2] + wrap_up(i2, geo.n[2]);
+    const float4 a = reinterpret_cast<const float4*>(src)[0], b = reinterpret_cast<const float4*>(src)[1];
+    float4 h, l;
+    float* o = out + inst * 4 * comp + (i0 * sd.P1 + i1) * sd.P2s + i2;
+    tc_split4(make_float4(a.x, a.z, b.x, b.z), h, l);
+    *reinterpret_cast<float4*>(o) = h;
+    *reinterpret_cast<float4*>(o + 2 * comp) = l;
+    tc_split4(make_float4(a.y, a.w, b.y, b.w), h, l);
+    *reinterpret_cast<float4*>(o + comp) = h;
+    *reinterpret_cast<float4*>(o + 3 * comp) = l;
+  }
 }
 
 // Position in this CTA's batch sequence: items c, c + G, ... (CTA c of G; items are
@@ -114,21 +153,22 @@ __device__ __forceinline__ ItRec it_load_rec(const ItCursor& c, int num_items, i
 }
 
 template <int W, int WIN>
-__global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const float2* __restrict__ g, float2* __restrict__ f,
-                                                             Geom geo, Tiling tl, Bins bins) {
-  constexpr int E1 = it_e1(W), CH = it_ch(W), NCOL = it_ncol(W), N = it_n(W);
+__global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const __grid_constant__ CUtensorMap tmap,
+                                                             float2* __restrict__ f, Geom geo, Tiling tl, Bins bins) {
+  constexpr int E1 = it_e1(W), CH = it_ch(W), NP = it_pairs(W);
   constexpr int E0MAX = kItMaxT0 + W - 1;
   constexpr int MAXCH = (E0MAX + CH - 1) / CH;
-  constexpr int PPAD = it_pairs_pad(W);
-  constexpr int BIT = (PPAD + kItBuilders * 8 - 1) / (kItBuilders * 8);  // pair blocks per builder warp
+  constexpr int GI = (NP + 15) / 16;  // 16-pair groups of the tensor-memory read-out
   constexpr int SH = off_bits(3);
   constexpr uint32_t MASK = (1u << SH) - 1u;
-  static_assert(NCOL <= 256 && N <= 256 && 2 * N <= 512, "two chunk accumulators must fit tensor memory");
+  constexpr uint32_t kBoxBytes = (uint32_t)(kItK * 4 * E1 * CH);
+  static_assert(NP <= 128, "a chunk's (plane, row) pairs must fit 128 B rows");
   static_assert(fixed_t_last(3, W) + W - 1 <= kItK, "innermost padded extent must fit K");
-  extern __shared__ __align__(16) unsigned char smem[];
-  const ItLayout L = it_layout(W);
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* smem = smem_raw + ((1024u - (tc::smem_u32(smem_raw) & 1023u)) & 1023u);
+  const ItLayout L = it_layout();
   uint64_t* afull = reinterpret_cast<uint64_t*>(smem + L.bar_off);  // [2] A of the batch built
-  uint64_t* bfull = afull + 2;                                       // [2] tile chunk built
+  uint64_t* bfull = afull + 2;                                       // [2] tile chunk landed (TMA)
   uint64_t* bempty = afull + 4;                                      // [2] MMAs of the chunk complete
   uint64_t* tfull = afull + 6;                                       // [2] accumulator complete
   uint64_t* tempty = afull + 8;                                      // [2] accumulator read out
@@ -141,11 +181,11 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const float2* __res
 
   if (tid == 0) {
     for (int i = 0; i < 2; ++i) {
-      tc::mbar_init(&afull[i], 4);             // one arrival per node warp
-      tc::mbar_init(&bfull[i], kItBuilders);   // one arrival per builder warp
+      tc::mbar_init(&afull[i], 4);    // one arrival per node warp
+      tc::mbar_init(&bfull[i], 1);    // the TMA thread's arrival (+ the boxes' bytes)
       tc::mbar_init(&bempty[i], 1);
       tc::mbar_init(&tfull[i], 1);
-      tc::mbar_init(&tempty[i], 4);            // one arrival per node warp
+      tc::mbar_init(&tempty[i], 4);   // one arrival per node warp
     }
     tc::mbar_fence_init();
   }
@@ -161,83 +201,44 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const float2* __res
 
   // Every role walks items c, c + G, ... (CTA c), batches of 128 nodes within an
   // item and nch chunks within a batch; chunk gc (counted across the CTA's whole
-  // sequence) uses tile buffer and accumulator gc & 1 in their cycle gc >> 1.
-  if (warp < kItBuilders) {
-    // ======================= builder warps: tile chunks =======================
-    const int pl8 = lane & 7, qq = lane >> 3;
-    const int64_t n0 = geo.n[0], n1 = geo.n[1], n2 = geo.n[2];
-    uint32_t gc = 0;
-    for (int it = blockIdx.x; it < num_items; it += G) {
-      const int4 item = bins.items[it];
-      const TileOrigin o = decode_tile<3>(geo, tl, item.x);
-      const float2* gi = g + o.inst * geo.ntot;
-      const int nbatch = (item.z - item.y + kItNodes - 1) / kItNodes;
-      for (int bt = 0; bt < nbatch; ++bt) {
-        for (int c = 0; c < nch; ++c, ++gc) {
-          const uint32_t buf = gc & 1u;
-          if (gc >= 2) healthy &= tc::mbar_wait_warp(&bempty[buf], ((gc >> 1) - 1u) & 1u, kItPolls);
-          unsigned char* bh = smem + L.b_off + buf * 2u * L.b_bytes;
-          unsigned char* bl = bh + L.b_bytes;
-          const int ps = c * CH, np = min(CH, E0 - ps);
-          // item (pair, quad): pair = (plane, row) of the chunk, quad = 4 consecutive p2;
-          // all of this thread's loads go out before the first conversion
-          float4 v[BIT][2][2];
-#pragma unroll
-          for (int i = 0; i < BIT; ++i) {
-            const int pair = warp * 8 + i * kItBuilders * 8 + pl8;
-            const int pl = pair / E1, p1 = pair - pl * E1;
-            const bool on = pl < np;
-            int64_t rowg = 0;
-            if (on) rowg = (wrap_up(o.a[0] + ps + pl, n0) * n1 + wrap_up(o.a[1] + p1, n1)) * n2;
-#pragma unroll
-            for (int qh = 0; qh < 2; ++qh) {
-              const int qd = qh * 4 + qq;  // p2 = 4 qd .. 4 qd + 3 (never straddles the wrap: n2 % 4 == 0)
-              v[i][qh][0] = v[i][qh][1] = make_float4(0.f, 0.f, 0.f, 0.f);
-              if (on) {
-                const float4* src = reinterpret_cast<const float4*>(gi + rowg + wrap_up(o.a[2] + 4 * qd, n2));
-                v[i][qh][0] = src[0];
-                v[i][qh][1] = src[1];
-              }
-            }
+  // sequence) uses chunk stage and accumulator gc & 1 in their cycle gc >> 1.
+  if (warp == kItTmaWarp) {
+    // ======================= TMA: tile chunks =======================
+    if (lane == 0) {
+      uint32_t gc = 0;
+      for (int it = blockIdx.x; it < num_items; it += G) {
+        const int4 item = bins.items[it];
+        const TileOrigin o = decode_tile<3>(geo, tl, item.x);
+        const int nbatch = (item.z - item.y + kItNodes - 1) / kItNodes;
+        for (int bt = 0; bt < nbatch; ++bt) {
+          for (int c = 0; c < nch; ++c, ++gc) {
+            const uint32_t buf = gc & 1u;
+            if (gc >= 2) healthy &= tc::mbar_wait_bounded(&bempty[buf], ((gc >> 1) - 1u) & 1u, kItPolls);
+            unsigned char* st = smem + L.b_off + buf * kItStage;
+            tc::mbar_arrive_expect_tx(&bfull[buf], 4u * kBoxBytes);
+            // x = o.a[2] is a multiple of the innermost tile extent (>= 4 floats: 16 bytes)
+            for (int comp = 0; comp < 4; ++comp)
+              tc::tma_load_5d(st + comp * kItPart, &tmap, (int)o.a[2], (int)o.a[1], (int)o.a[0] + c * CH, comp,
+                              (int)o.inst, &bfull[buf]);
           }
-#pragma unroll
-          for (int i = 0; i < BIT; ++i) {
-            const int pair = warp * 8 + i * kItBuilders * 8 + pl8;
-            if (pair < PPAD) {
-#pragma unroll
-              for (int qh = 0; qh < 2; ++qh) {
-                const int qd = qh * 4 + qq;
-                const float4 v0 = v[i][qh][0], v1 = v[i][qh][1];
-                const float4 re = make_float4(v0.x, v0.z, v1.x, v1.z), im = make_float4(v0.y, v0.w, v1.y, v1.w);
-                float4 h, l;
-                const int nr = 2 * pair;
-                const uint32_t ore = (uint32_t)(nr >> 3) * kItSBOB + (uint32_t)qd * kItLBO + (uint32_t)(nr & 7) * 16u;
-                const uint32_t oim = ore + 16u;  // row 2 pair + 1: same group (nr even)
-                tc_split4(re, h, l);
-                *reinterpret_cast<float4*>(bh + ore) = h;
-                *reinterpret_cast<float4*>(bl + ore) = l;
-                tc_split4(im, h, l);
-                *reinterpret_cast<float4*>(bh + oim) = h;
-                *reinterpret_cast<float4*>(bl + oim) = l;
-              }
-            }
-          }
-          tc::fence_proxy_async_smem();
-          tc::mbar_arrive_warp(&bfull[buf]);
         }
       }
+      // the boxes of the last two chunks have landed before this CTA can exit
+      if (gc >= 1) healthy &= tc::mbar_wait_bounded(&bfull[(gc - 1) & 1u], ((gc - 1) >> 1) & 1u, kItPolls);
+      if (gc >= 2) healthy &= tc::mbar_wait_bounded(&bfull[(gc - 2) & 1u], ((gc - 2) >> 1) & 1u, kItPolls);
     }
+    __syncwarp();
   } else if (warp == kItMmaWarp) {
     // ======================= MMA issuer: lane 0 =======================
     if (lane == 0) {
       const uint32_t sa = tc::smem_u32(smem + L.a_off), sb = tc::smem_u32(smem + L.b_off);
-      const uint64_t d_abuf = (uint64_t)((2u * L.a_bytes) >> 4);  // A buffer 1 = buffer 0 + d_abuf
+      const uint64_t d_abuf = (uint64_t)(32768u >> 4);  // A buffer 1 = buffer 0 + d_abuf
       const uint64_t d_ah = tc::smem_desc(sa, kItLBO, kItSBOA);
-      const uint64_t d_al = tc::smem_desc(sa + L.a_bytes, kItLBO, kItSBOA);
-      const uint64_t d_bh = tc::smem_desc(sb, kItLBO, kItSBOB);
-      const uint64_t d_bl = tc::smem_desc(sb + L.b_bytes, kItLBO, kItSBOB);
-      const uint64_t d_buf = (uint64_t)((2u * L.b_bytes) >> 4);  // buffer 1 = buffer 0 + d_buf
-      const uint32_t idesc = tc::idesc_tf32(128, N);
+      const uint64_t d_al = tc::smem_desc(sa + 16384u, kItLBO, kItSBOA);
+      const uint64_t d_bh = tc::smem_desc_sw128(sb);
+      const uint64_t d_bl = tc::smem_desc_sw128(sb + 2u * kItPart);
+      const uint64_t d_buf = (uint64_t)(kItStage >> 4);  // stage 1 = stage 0 + d_buf
+      const uint32_t idesc = tc::idesc_tf32(128, 256);
       uint32_t gc = 0, gbt = 0;
       for (int it = blockIdx.x; it < num_items; it += G) {
         const int4 item = bins.items[it];
@@ -255,10 +256,11 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const float2* __res
             const uint64_t bo = buf ? d_buf : 0ull;
 #pragma unroll
             for (int ks = 0; ks < kItK / 8; ++ks) {
-              const uint64_t ko = (uint64_t)((ks * 2 * kItLBO) >> 4);
-              tc::mma_tf32(d, d_ah + ao + ko, d_bh + bo + ko, idesc, ks > 0 ? 1u : 0u);
-              tc::mma_tf32(d, d_ah + ao + ko, d_bl + bo + ko, idesc, 1u);
-              tc::mma_tf32(d, d_al + ao + ko, d_bh + bo + ko, idesc, 1u);
+              const uint64_t ka = (uint64_t)((ks * 2 * kItLBO) >> 4);  // A: two core matrices per k-step
+              const uint64_t kb = (uint64_t)((ks * 32) >> 4);          // B: 32 bytes into the swizzled row
+              tc::mma_tf32(d, d_ah + ao + ka, d_bh + bo + kb, idesc, ks > 0 ? 1u : 0u);
+              tc::mma_tf32(d, d_ah + ao + ka, d_bl + bo + kb, idesc, 1u);
+              tc::mma_tf32(d, d_al + ao + ka, d_bh + bo + kb, idesc, 1u);
             }
             tc::mma_commit(&bempty[buf]);
             tc::mma_commit(&tfull[buf]);
@@ -281,8 +283,8 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const float2* __res
     const float mf = (float)geo.m;
     const TapK k0 = tap_k<WIN>(geo, 0), k1 = tap_k<WIN>(geo, 1), k2 = tap_k<WIN>(geo, 2);
     auto build_a = [&](const ItRec& r, uint32_t ab) {
-      unsigned char* ah = smem + L.a_off + ab * 2u * L.a_bytes;
-      unsigned char* al = ah + L.a_bytes;
+      unsigned char* ah = smem + L.a_off + ab * 32768u;
+      unsigned char* al = ah + 16384u;
       const int o2 = (int)(r.off >> (2 * SH));
 #pragma unroll
       for (int k4 = 0; k4 < kItK / 4; ++k4) {
@@ -328,19 +330,20 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const float2* __res
           tc::fence_after_sync();
           const uint32_t t0 = tmem + ((uint32_t)(32 * q) << 16) + buf * 256u;
 #pragma unroll
-          for (int gi = 0; gi < N / 16; ++gi) {
-            float v[16];
-            tc::tmem_ld16(t0 + (uint32_t)(gi * 16), v);
+          for (int gi = 0; gi < GI; ++gi) {
+            float vr[16], vi[16];
+            tc::tmem_ld16(t0 + (uint32_t)(gi * 16), vr);         // real parts of pairs 16 gi ..
+            tc::tmem_ld16(t0 + 128u + (uint32_t)(gi * 16), vi);  // imaginary parts
             tc::tmem_ld_wait();
 #pragma unroll
-            for (int u = 0; u < 16; u += 2) {
-              const int col = gi * 16 + u;  // (re, im) of (plane pl, row p1)
-              if (col < NCOL) {
-                const int pl = col / (2 * E1), p1 = (col % (2 * E1)) / 2;
+            for (int u = 0; u < 16; ++u) {
+              const int pr = gi * 16 + u;  // (plane pl, row p1) of the chunk
+              if (pr < NP) {
+                const int pl = pr / E1, p1 = pr - (pr / E1) * E1;
                 if (c * CH + pl < E0MAX) {
                   const float w = w0x[c * CH + pl] * w1x[p1];
-                  accx = fmaf(w, v[u], accx);
-                  accy = fmaf(w, v[u + 1], accy);
+                  accx = fmaf(w, vr[u], accx);
+                  accy = fmaf(w, vi[u], accy);
                 }
               }
             }

@@ -435,6 +435,7 @@ void plan_release(Plan* p) {
       p->gexec[i] = nullptr;
     }
   free_bins(p);
+  interp_tc_release(*p);
   cudaFree(p->bins.inst_off);
   cudaFree(p->bins.work);
   cudaFree(p->bins.num_items);
@@ -536,9 +537,26 @@ static void rec(Plan* p, int i) {
   if (p->timing) cudaEventRecord(p->ev[i], p->stream);
 }
 
+// Buffers of the tensor-core interpolation (the grid's split planes and their TMA
+// map), created before its first launch.  When they cannot be created and the kernel
+// was chosen automatically, the shared-tile interpolation runs instead.
+static int prepare_interp(Plan* p) {
+  if (p->tl.interp_kernel != CUNFFT_X_INTERP_TENSOR || p->it_ready) return CUNFFT_X_SUCCESS;
+  const cudaError_t e = interp_tc_prepare(*p);
+  if (e == cudaSuccess) return CUNFFT_X_SUCCESS;
+  cudaGetLastError();  // a failed allocation leaves no sticky error
+  if (p->interp_mode == CUNFFT_X_INTERP_AUTO) {
+    p->tl.interp_kernel = CUNFFT_X_INTERP_SHARED;
+    ++p->node_gen;
+    return CUNFFT_X_SUCCESS;
+  }
+  return check_cuda(p, e, "tensor-core interpolation buffers");
+}
+
 int plan_forward(Plan* p, const void* fhat, void* f) {
   if (!p->nodes_set) return set_status(p, CUNFFT_X_NODES_NOT_SET, "forward: nodes not set");
   if (!p->bins.valid) CG_TRY(rebin(p));
+  CG_TRY(prepare_interp(p));
   rec(p, 0);
   CG_TRY(check_cuda(p, launch_roc_forward(*p, fhat, p->g, p->stream), "roll-off kernel"));
   rec(p, 1);
@@ -606,6 +624,7 @@ int plan_run_graph(Plan* p, int adjoint, const void* in, void* out) {
 int plan_interp_only(Plan* p, const void* g, void* f) {
   if (!p->nodes_set) return set_status(p, CUNFFT_X_NODES_NOT_SET, "interp: nodes not set");
   if (!p->bins.valid) CG_TRY(rebin(p));
+  CG_TRY(prepare_interp(p));
   CG_TRY(check_cuda(p, launch_interp(*p, g, f, p->stream), "interpolation kernel"));
   return set_status(p, CUNFFT_X_SUCCESS, nullptr);
 }
@@ -672,6 +691,10 @@ int plan_autotune(Plan* p, int reps) {
   bool failed = false;
   // device time of reps launches of one gridding kernel (after one warm-up); < 0 on failure
   auto time_kernel = [&](bool spread) -> float {
+    if (!spread && p->tl.interp_kernel == CUNFFT_X_INTERP_TENSOR && interp_tc_prepare(*p) != cudaSuccess) {
+      cudaGetLastError();
+      return -1.f;
+    }
     auto run = [&]() {
       return spread ? launch_spread(*p, scratch_f, p->g, p->stream) : launch_interp(*p, p->g, scratch_f, p->stream);
     };

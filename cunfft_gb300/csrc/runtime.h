@@ -7,6 +7,7 @@
 // state, so any number of plans coexist and run concurrently on their streams.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <cufft.h>
 #include <stdint.h>
@@ -61,6 +62,11 @@ struct Plan {
   uint64_t g_gen[2] = {0, 0};
   uint64_t node_gen = 0;  // bumped by every node binding / tiling change
   HostPath* hp = nullptr; // created by the first host-buffer transform
+  // tensor-core interpolation: the grid's padded TF32 hi/lo planes and their TMA map,
+  // created before its first launch (interp_tc_prepare)
+  float* it_split = nullptr;
+  CUtensorMap it_tmap{};
+  bool it_ready = false;
 };
 
 inline size_t plan_elem_bytes(const Plan* p) { return p->prec == kF64 ? 16 : 8; }
@@ -117,6 +123,8 @@ cudaError_t grid_launch_spread_tc(const Plan& p, const void* f, void* g, cudaStr
 // tensor-core interpolation kernel (grid_interp_tc.cu)
 bool interp_tc_supported(const Plan& p);
 cudaError_t grid_launch_interp_tc(const Plan& p, const void* g, void* f, cudaStream_t st);
+cudaError_t interp_tc_prepare(Plan& p);
+void interp_tc_release(Plan& p);
 
 // launchers (kernel .cu files); all asynchronous on st
 cudaError_t launch_binning(const Plan& p, const double* x, cudaStream_t st);

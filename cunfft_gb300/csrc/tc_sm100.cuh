@@ -25,6 +25,17 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint
          ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
 }
 
+// K-major operand in the 128-byte swizzled layout written by a TMA load with
+// CU_TENSOR_MAP_SWIZZLE_128B: rows of 128 bytes (32 TF32 K values), 8-row atoms of
+// 1024 bytes (SBO), the 16-byte chunks of row r XOR-permuted by r mod 8.  The leading
+// byte offset is unused (K fits one atom), the layout type 2 (128-byte swizzle) sits
+// in bits 61-63.  The atoms must start on 1024-byte boundaries; the k-th group of 8
+// K values starts 32 k bytes into the row (the hardware applies the XOR).
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t saddr) {
+  return (uint64_t)((saddr & 0x3FFFFu) >> 4) | (1ull << 16) | ((uint64_t)(1024u >> 4) << 32) | (1ull << 46) |
+         (2ull << 61);
+}
+
 // ---- instruction descriptor: kind::tf32, FP32 accumulator, A and B K-major ----
 __host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
   return (1u << 4)                        // D format: F32
@@ -71,6 +82,23 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
 // arrive (release) on the mbarrier once
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// Arrival that also announces `bytes` of asynchronous (TMA) transactions on the barrier.
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+// 5-D tiled TMA load of one box into shared memory, completing `bar`'s transactions.
+// c0 (the innermost coordinate) times the element size must be a multiple of 16 bytes.
+__device__ __forceinline__ void tma_load_5d(void* dst, const void* tmap, int c0, int c1, int c2, int c3, int c4,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, "
+      "%6}], [%7];\n" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(tmap)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(smem_u32(bar))
+      : "memory");
 }
 
 // Warp-wide hand-offs on an mbarrier whose count is in warps: one arrival or one
