@@ -454,8 +454,10 @@ def run_ours(args):
                 "rel_l2_vs_device_path": e2e_err},
         "roofline": roofline,
         # binning 4 (count, scan, scatter, items) + forward 2 (roll-off, interpolation)
-        # + adjoint 2 (spreading, roll-off) + the sample permutation of the tensor-core spreading
-        "gpu_launches": args.steps * (8 + (1 if p32.spread_kernel() == "tensor" else 0)),
+        # + adjoint 2 (spreading, roll-off) + the sample permutation of the tensor-core
+        # spreading + the grid split of the tensor-core interpolation
+        "gpu_launches": args.steps * (8 + (1 if p32.spread_kernel() == "tensor" else 0)
+                                      + (1 if p32.interp_kernel() == "tensor" else 0)),
         "clocks": clk,
     }
     if cpu is not None:

@@ -139,6 +139,7 @@ struct Bins {
   void*    fperm;        // [M] complex: the samples in sorted order (filled per call by the tensor-core spreading)
   int32_t* inst_off;     // [batch + 1] node offsets per instance
   int32_t* status;       // [1] device-side error flag
+  uint32_t* fmax;        // [1] largest |Re|, |Im| of the samples being spread (float bits), per call
   int64_t  M;            // total nodes
   int64_t  max_items;
   int      valid;        // nodes binned for the current tiling

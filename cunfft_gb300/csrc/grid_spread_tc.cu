@@ -36,7 +36,9 @@ static cudaError_t launch_tc(const Plan& p, const void* in, void* out, cudaStrea
   // samples in sorted order, read contiguously by the kernel's record loads
   const int64_t M = p.bins.M;
   const int pblocks = (int)std::min<int64_t>((M + 255) / 256, (int64_t)p.num_sms * 16);
-  k_permute_samples<<<pblocks, 256, 0, st>>>((const float2*)in, p.bins.sidx, M, (float2*)p.bins.fperm);
+  cudaError_t em = cudaMemsetAsync(p.bins.fmax, 0, sizeof(uint32_t), st);
+  if (em != cudaSuccess) return em;
+  k_permute_samples<<<pblocks, 256, 0, st>>>((const float2*)in, p.bins.sidx, M, (float2*)p.bins.fperm, p.bins.fmax);
   kern<<<p.num_sms * per_sm, kTcThreads, smem, st>>>((const float2*)in, (float2*)out, p.geo, p.tl, p.bins);
   return cudaGetLastError();
 }

@@ -8,8 +8,8 @@
 // and H is the product D = A B^T of
 //     A[j, p2]              = w2_j[p2 - o2_j]                  (128 nodes x 32 columns)
 //     B[(re|im, p0, p1), p2] = Re|Im G[p0, p1, p2]             (the tile, K = p2)
-// computed in chunks of kItCh planes (the chunk's CH E1 (plane, row) pairs are B rows
-// 0.. of the real part and 128.. of the imaginary part: N = 256), two chunk
+// computed in chunks of CH planes (the chunk's CH E1 <= 64 (plane, row) pairs are B
+// rows 0.. of the real part and 64.. of the imaginary part: N = 128), four chunk
 // accumulators in tensor memory.  D lives in tensor memory with node j in lane j, so
 // the thread that owns node j finishes the w0 (x) w1 sum over its window from its own
 // lane, chunk by chunk, in registers.
@@ -20,7 +20,7 @@
 // arrays (no wrap), and one thread loads each chunk with four TMA boxes (hi re, hi im,
 // lo re, lo im; 32 floats x E1 rows x CH planes) straight into the 128-byte swizzled
 // K-major layout the MMAs read.  Warp roles: warp 0 lane 0 issues the TMA loads
-// (two chunk stages), warp 1 lane 0 the MMAs hi*hi + hi*lo + lo*hi per k-step of 8
+// (four chunk stages), warp 1 lane 0 the MMAs hi*hi + hi*lo + lo*hi per k-step of 8
 // columns, warps 2-5 (lane quarters) build A from their nodes' taps and reduce D.
 // Hand-offs are mbarriers (the chunk stages' with TMA transaction counts); every wait
 // is bounded and a wait that gives up sets the plan's device status flag.
@@ -42,13 +42,16 @@ constexpr int kItNodeWarp0 = 2;    // 4 node warps: lane quarter = warp % 4
 constexpr int kItThreads = 6 * 32;
 constexpr uint32_t kItLBO = 128;               // A: core matrices along K
 constexpr uint32_t kItSBOA = 1024;             // A: 8-row groups (32 K values = 8 core matrices)
-constexpr uint32_t kItPart = 16384;            // one B part (hi re, hi im, lo re, lo im): 128 rows x 128 bytes
+constexpr int kItHalf = 64;                    // B rows per part: real parts 0..63, imaginary 64..127
+constexpr int kItN = 2 * kItHalf;              // MMA N
+constexpr int kItStages = 4;                   // chunk stages = tensor-memory accumulators (kItN columns each)
+constexpr uint32_t kItPart = kItHalf * 128;    // one B part (hi re, hi im, lo re, lo im): 64 rows x 128 bytes
 constexpr uint32_t kItStage = 4 * kItPart;     // one chunk stage: B hi = parts 0-1, B lo = parts 2-3
 constexpr uint32_t kItPolls = 1u << 20;        // mbarrier polls (<= 1 us each) before giving up
 
 __host__ __device__ constexpr int it_e1(int W) { return fixed_t_mid(3, W) + W - 1; }
-__host__ __device__ constexpr int it_ch(int W) { return 128 / it_e1(W); }                     // planes per chunk
-__host__ __device__ constexpr int it_pairs(int W) { return it_ch(W) * it_e1(W); }            // (plane, row) pairs <= 128
+__host__ __device__ constexpr int it_ch(int W) { return kItHalf / it_e1(W); }                 // planes per chunk
+__host__ __device__ constexpr int it_pairs(int W) { return it_ch(W) * it_e1(W); }            // (plane, row) pairs <= 64
 
 __host__ __device__ constexpr bool interp_tc_ok(int d, int W, int T0, int64_t n2) {
   return d == 3 && W >= 4 && W <= 16 && T0 >= 1 && T0 <= kItMaxT0 && n2 >= 4 && n2 % 4 == 0;
@@ -56,16 +59,16 @@ __host__ __device__ constexpr bool interp_tc_ok(int d, int W, int T0, int64_t n2
 
 // Shared-memory layout (byte offsets from a 1024-byte aligned base; host and device agree).
 struct ItLayout {
-  uint32_t b_off;      // 2 chunk stages of kItStage
+  uint32_t b_off;      // kItStages chunk stages of kItStage
   uint32_t a_off;      // 2 buffers x (A hi, A lo), 16 KB each
-  uint32_t bar_off;    // afull[2], bfull[2], bempty[2], tfull[2], tempty[2]; tensor-memory base
+  uint32_t bar_off;    // afull[2], bfull[4], bempty[4], tfull[4], tempty[4]; tensor-memory base
   uint32_t total;      // bytes past the aligned base
   uint32_t dyn;        // dynamic shared memory to request (alignment slack included)
 };
 
 __host__ __device__ constexpr ItLayout it_layout() {
-  return ItLayout{0u, 2u * kItStage, 2u * kItStage + 4u * 16384u, 2u * kItStage + 4u * 16384u + 96u,
-                  2u * kItStage + 4u * 16384u + 96u + 1024u};
+  return ItLayout{0u, kItStages * kItStage, kItStages * kItStage + 4u * 16384u,
+                  kItStages * kItStage + 4u * 16384u + 160u, kItStages * kItStage + 4u * 16384u + 160u + 1024u};
 }
 
 // Padded split planes of the grid: float [batch][4][P0][P1][P2s], component 0 hi re,
@@ -162,17 +165,18 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const __grid_consta
   constexpr int SH = off_bits(3);
   constexpr uint32_t MASK = (1u << SH) - 1u;
   constexpr uint32_t kBoxBytes = (uint32_t)(kItK * 4 * E1 * CH);
-  static_assert(NP <= 128, "a chunk's (plane, row) pairs must fit 128 B rows");
+  static_assert(NP <= kItHalf && NP > 0, "a chunk's (plane, row) pairs must fit one B part");
+  static_assert(kItStages * kItN <= 512, "the accumulators must fit tensor memory");
   static_assert(fixed_t_last(3, W) + W - 1 <= kItK, "innermost padded extent must fit K");
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = smem_raw + ((1024u - (tc::smem_u32(smem_raw) & 1023u)) & 1023u);
   const ItLayout L = it_layout();
   uint64_t* afull = reinterpret_cast<uint64_t*>(smem + L.bar_off);  // [2] A of the batch built
-  uint64_t* bfull = afull + 2;                                       // [2] tile chunk landed (TMA)
-  uint64_t* bempty = afull + 4;                                      // [2] MMAs of the chunk complete
-  uint64_t* tfull = afull + 6;                                       // [2] accumulator complete
-  uint64_t* tempty = afull + 8;                                      // [2] accumulator read out
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + L.bar_off + 80);
+  uint64_t* bfull = afull + 2;                                       // [4] tile chunk landed (TMA)
+  uint64_t* bempty = afull + 6;                                      // [4] MMAs of the chunk complete
+  uint64_t* tfull = afull + 10;                                      // [4] accumulator complete
+  uint64_t* tempty = afull + 14;                                     // [4] accumulator read out
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + L.bar_off + 144);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int E0 = tl.E[0];
   const int nch = (E0 + CH - 1) / CH;
@@ -180,8 +184,8 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const __grid_consta
   const int G = (int)gridDim.x;
 
   if (tid == 0) {
-    for (int i = 0; i < 2; ++i) {
-      tc::mbar_init(&afull[i], 4);    // one arrival per node warp
+    for (int i = 0; i < 2; ++i) tc::mbar_init(&afull[i], 4);  // one arrival per node warp
+    for (int i = 0; i < kItStages; ++i) {
       tc::mbar_init(&bfull[i], 1);    // the TMA thread's arrival (+ the boxes' bytes)
       tc::mbar_init(&bempty[i], 1);
       tc::mbar_init(&tfull[i], 1);
@@ -201,7 +205,7 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const __grid_consta
 
   // Every role walks items c, c + G, ... (CTA c), batches of 128 nodes within an
   // item and nch chunks within a batch; chunk gc (counted across the CTA's whole
-  // sequence) uses chunk stage and accumulator gc & 1 in their cycle gc >> 1.
+  // sequence) uses chunk stage and accumulator gc & 3 in their cycle gc >> 2.
   if (warp == kItTmaWarp) {
     // ======================= TMA: tile chunks =======================
     if (lane == 0) {
@@ -212,8 +216,8 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const __grid_consta
         const int nbatch = (item.z - item.y + kItNodes - 1) / kItNodes;
         for (int bt = 0; bt < nbatch; ++bt) {
           for (int c = 0; c < nch; ++c, ++gc) {
-            const uint32_t buf = gc & 1u;
-            if (gc >= 2) healthy &= tc::mbar_wait_bounded(&bempty[buf], ((gc >> 1) - 1u) & 1u, kItPolls);
+            const uint32_t buf = gc & 3u;
+            if (gc >= 4) healthy &= tc::mbar_wait_bounded(&bempty[buf], ((gc >> 2) - 1u) & 1u, kItPolls);
             unsigned char* st = smem + L.b_off + buf * kItStage;
             tc::mbar_arrive_expect_tx(&bfull[buf], 4u * kBoxBytes);
             // x = o.a[2] is a multiple of the innermost tile extent (>= 4 floats: 16 bytes)
@@ -223,9 +227,9 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const __grid_consta
           }
         }
       }
-      // the boxes of the last two chunks have landed before this CTA can exit
-      if (gc >= 1) healthy &= tc::mbar_wait_bounded(&bfull[(gc - 1) & 1u], ((gc - 1) >> 1) & 1u, kItPolls);
-      if (gc >= 2) healthy &= tc::mbar_wait_bounded(&bfull[(gc - 2) & 1u], ((gc - 2) >> 1) & 1u, kItPolls);
+      // the boxes of the last chunks have landed before this CTA can exit
+      for (uint32_t k = 1; k <= (uint32_t)kItStages && k <= gc; ++k)
+        healthy &= tc::mbar_wait_bounded(&bfull[(gc - k) & 3u], ((gc - k) >> 2) & 1u, kItPolls);
     }
     __syncwarp();
   } else if (warp == kItMmaWarp) {
@@ -237,8 +241,8 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const __grid_consta
       const uint64_t d_al = tc::smem_desc(sa + 16384u, kItLBO, kItSBOA);
       const uint64_t d_bh = tc::smem_desc_sw128(sb);
       const uint64_t d_bl = tc::smem_desc_sw128(sb + 2u * kItPart);
-      const uint64_t d_buf = (uint64_t)(kItStage >> 4);  // stage 1 = stage 0 + d_buf
-      const uint32_t idesc = tc::idesc_tf32(128, 256);
+      const uint64_t d_buf = (uint64_t)(kItStage >> 4);  // stage k = stage 0 + k d_buf
+      const uint32_t idesc = tc::idesc_tf32(128, kItN);
       uint32_t gc = 0, gbt = 0;
       for (int it = blockIdx.x; it < num_items; it += G) {
         const int4 item = bins.items[it];
@@ -248,12 +252,12 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const __grid_consta
           healthy &= tc::mbar_wait_bounded(&afull[ab], (gbt >> 1) & 1u, kItPolls);
           const uint64_t ao = ab ? d_abuf : 0ull;
           for (int c = 0; c < nch; ++c, ++gc) {
-            const uint32_t buf = gc & 1u;
-            healthy &= tc::mbar_wait_bounded(&bfull[buf], (gc >> 1) & 1u, kItPolls);
-            if (gc >= 2) healthy &= tc::mbar_wait_bounded(&tempty[buf], ((gc >> 1) - 1u) & 1u, kItPolls);
+            const uint32_t buf = gc & 3u;
+            healthy &= tc::mbar_wait_bounded(&bfull[buf], (gc >> 2) & 1u, kItPolls);
+            if (gc >= 4) healthy &= tc::mbar_wait_bounded(&tempty[buf], ((gc >> 2) - 1u) & 1u, kItPolls);
             tc::fence_after_sync();
-            const uint32_t d = tmem + buf * 256u;
-            const uint64_t bo = buf ? d_buf : 0ull;
+            const uint32_t d = tmem + buf * (uint32_t)kItN;
+            const uint64_t bo = (uint64_t)buf * d_buf;
 #pragma unroll
             for (int ks = 0; ks < kItK / 8; ++ks) {
               const uint64_t ka = (uint64_t)((ks * 2 * kItLBO) >> 4);  // A: two core matrices per k-step
@@ -267,9 +271,9 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const __grid_consta
           }
         }
       }
-      // the last chunk commits are waited by the node warps; the last bempty arrivals by nobody
-      if (gc >= 1) healthy &= tc::mbar_wait_bounded(&bempty[(gc - 1) & 1u], ((gc - 1) >> 1) & 1u, kItPolls);
-      if (gc >= 2) healthy &= tc::mbar_wait_bounded(&bempty[(gc - 2) & 1u], ((gc - 2) >> 1) & 1u, kItPolls);
+      // the last chunk commits are waited by the node warps; the last bempty arrivals here
+      for (uint32_t k = 1; k <= (uint32_t)kItStages && k <= gc; ++k)
+        healthy &= tc::mbar_wait_bounded(&bempty[(gc - k) & 3u], ((gc - k) >> 2) & 1u, kItPolls);
     }
     __syncwarp();
   } else {
@@ -325,15 +329,15 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const __grid_consta
 #pragma unroll
       for (int c = 0; c < MAXCH; ++c) {
         if (c < nch) {
-          const uint32_t buf = gc & 1u;
-          healthy &= tc::mbar_wait_warp(&tfull[buf], (gc >> 1) & 1u, kItPolls);
+          const uint32_t buf = gc & 3u;
+          healthy &= tc::mbar_wait_warp(&tfull[buf], (gc >> 2) & 1u, kItPolls);
           tc::fence_after_sync();
-          const uint32_t t0 = tmem + ((uint32_t)(32 * q) << 16) + buf * 256u;
+          const uint32_t t0 = tmem + ((uint32_t)(32 * q) << 16) + buf * (uint32_t)kItN;
 #pragma unroll
           for (int gi = 0; gi < GI; ++gi) {
             float vr[16], vi[16];
             tc::tmem_ld16(t0 + (uint32_t)(gi * 16), vr);         // real parts of pairs 16 gi ..
-            tc::tmem_ld16(t0 + 128u + (uint32_t)(gi * 16), vi);  // imaginary parts
+            tc::tmem_ld16(t0 + (uint32_t)kItHalf + (uint32_t)(gi * 16), vi);  // imaginary parts
             tc::tmem_ld_wait();
 #pragma unroll
             for (int u = 0; u < 16; ++u) {

@@ -1,4 +1,4 @@
-// kernels_spread_tc.cuh -- 3D FP32 spreading on the tensor cores (tcgen05, 3xTF32).
+// kernels_spread_tc.cuh -- 3D FP32 spreading on the tensor cores (tcgen05, 3 x FP16).
 //
 // Same work items, tiles and weights as k_spread (kernels_grid.cuh).  For a tile
 // with padded extents E0 x E1 x E2 and a batch of K nodes, the update
@@ -12,12 +12,16 @@
 // Warp roles: 15 builder warps and one MMA warp.  Per batch of kTcK = 16 nodes the
 // builders (1) evaluate w0 and w1 over the padded planes/rows and build B, then,
 // after one named barrier among themselves, (2) build A; operands are split into
-// TF32 hi + lo parts (hi = tf32(v), lo = v - hi), and the thread mappings write 128
-// contiguous bytes per 8-lane store phase (no bank conflicts).  Each builder
-// thread then arrives on the stage's `full` mbarrier; lane 0 of the MMA warp waits
-// on it and issues, per M-tile and k-step of 8 nodes, the three MMAs
-// hi*hi + hi*lo + lo*hi (FP32 accuracy, error ~2^-22 relative per product), then
-// commits them to the stage's `empty` mbarrier.  Operands have 3 stages where
+// FP16 hi + lo parts (hi = fp16(v), lo = fp16(v - hi): 11 + 11 significant bits,
+// the precision of a TF32 hi + lo split), and the thread mappings write 128
+// contiguous bytes per 8-lane store phase (no bank conflicts).  FP16's range is
+// kept by powers of two: A (weights in [0, 1]) is scaled by 2^10, B by 2^(14 - e)
+// where 2^e bounds |w2 f norm| over the call's samples (their largest |Re|, |Im|,
+// found by k_permute_samples), and the epilogue scales the sums back exactly.
+// Each builder thread then arrives on the stage's `full` mbarrier; lane 0 of the
+// MMA warp waits on it and issues, per M-tile, the three kind::f16 MMAs (K = 16
+// nodes) hi*hi + hi*lo + lo*hi with FP32 accumulation (error ~2^-22 relative per
+// product), then commits them to the stage's `empty` mbarrier.  Operands have 3 stages where
 // shared memory allows, else 2 (builders wait on `empty` before reusing a stage);
 // node records are loaded two batches ahead and staged one batch ahead.
 // At the end of a work item the accumulators go TMEM -> registers -> a shared-
@@ -30,13 +34,15 @@
 // memory so that the CTAs resident on one SM never ask for more than 512 columns.
 #pragma once
 
+#include <cuda_fp16.h>
+
 #include "kernels_grid.cuh"
 #include "tc_sm100.cuh"
 
 namespace cg {
 
 constexpr int kTcMaxT0 = 16;     // outer tile extent limit (E0 <= 31 planes)
-constexpr int kTcK = 16;         // nodes per staged batch: two TF32 k-steps of 8
+constexpr int kTcK = 16;         // nodes per staged batch: one FP16 MMA k-step of 16
 constexpr int kTcBuilders = 15;                  // warps that build operands
 constexpr int kTcMmaWarp = kTcBuilders;           // lane 0 issues the MMAs
 constexpr int kTcEpiWarp0 = kTcBuilders + 1;      // 4 epilogue warps: TMEM lane quarters 0..3
@@ -51,8 +57,10 @@ constexpr int kTcWxStride = 20;  // floats per expanded-weight row: 8 consecutiv
 constexpr int kTcRing = 4;
 constexpr int kTcAhead = kTcRing - 1;
 constexpr uint32_t kTcSlotOff = 0, kTcSlotFrac = kTcK * 4, kTcSlotVal = kTcK * 16, kTcSlotBytes = kTcK * 24;
-constexpr uint32_t kTcLBO = 128;                // core matrices along K
-constexpr uint32_t kTcSBO = (kTcK / 4) * 128;   // 8-row groups
+constexpr uint32_t kTcLBO = 128;                // core matrices (8 rows x 8 FP16) along K
+constexpr uint32_t kTcSBO = (kTcK / 8) * 128;   // 8-row groups
+constexpr float kTcScaleA = 1024.f;             // A = w0 w1 in [0, 1] -> [0, 2^10]
+constexpr int kTcLogB = 14;                     // |B| scaled to below 2^14
 constexpr uint32_t kTcPolls = 1u << 20;         // mbarrier polls (<= 1 us each) before giving up
 
 __host__ __device__ constexpr bool spread_tc_ok(int d, int W, int T0) {
@@ -79,8 +87,8 @@ __host__ __device__ inline TcLayout tc_layout(int W, int E0) {
   const int E1 = fixed_t_mid(3, W) + W - 1;
   const int rows = E0 * E1;
   L.mt = (rows + 127) / 128;
-  L.a_bytes = (uint32_t)L.mt * 128u * kTcK * 4u;
-  const uint32_t b_bytes = kTcN * kTcK * 4u;
+  L.a_bytes = (uint32_t)L.mt * 128u * kTcK * 2u;
+  const uint32_t b_bytes = kTcN * kTcK * 2u;
   L.stage_bytes = 2u * L.a_bytes + 2u * b_bytes;
   for (L.ns = 3; L.ns >= 2; --L.ns) {  // 3 operand stages when they fit in 227 KB
     const uint32_t ops = ((uint32_t)L.ns * L.stage_bytes + 1023u) & ~1023u;
@@ -98,9 +106,32 @@ __host__ __device__ inline TcLayout tc_layout(int W, int E0) {
   return L;
 }
 
-// byte offset of element (row 8 rg + ri, node group kg) in a K-major no-swizzle operand
+// byte offset of the 8 FP16 values (row 8 rg + ri, nodes 8 kg .. 8 kg + 7) in a K-major
+// no-swizzle operand
 __device__ __forceinline__ uint32_t tc_elem_off(int rg, int ri, int kg) {
   return (uint32_t)rg * kTcSBO + (uint32_t)kg * kTcLBO + (uint32_t)ri * 16u;
+}
+
+// 8 FP32 values -> FP16 hi (8 halves) and lo = fp16(v - hi) (8 halves)
+__device__ __forceinline__ void tc_split8_f16(const float* v, uint4& hi, uint4& lo) {
+  uint32_t h[4], l[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const __half2 hh = __floats2half2_rn(v[2 * i], v[2 * i + 1]);
+    const float2 hf = __half22float2(hh);
+    const __half2 ll = __floats2half2_rn(v[2 * i] - hf.x, v[2 * i + 1] - hf.y);
+    h[i] = *reinterpret_cast<const uint32_t*>(&hh);
+    l[i] = *reinterpret_cast<const uint32_t*>(&ll);
+  }
+  hi = make_uint4(h[0], h[1], h[2], h[3]);
+  lo = make_uint4(l[0], l[1], l[2], l[3]);
+}
+
+// 2^(kTcLogB - e), 2^e >= the call's largest |w2 f norm| (w2 <= 1): the B scale
+__device__ __forceinline__ float tc_scale_b(const Bins& bins, float norm) {
+  int e = 0;
+  frexpf(__uint_as_float(*bins.fmax) * norm, &e);
+  return ldexpf(1.f, kTcLogB - e);
 }
 
 
@@ -142,11 +173,18 @@ template <int N>
 __device__ __forceinline__ void cp_async_wait_group() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
 // Samples in sorted order (fp[k] = f[sidx[k]]), so that the spreading kernel's
-// per-batch record loads are contiguous.
+// per-batch record loads are contiguous, and their largest |Re|, |Im| into *fmax
+// (float bits: the unsigned order of non-negative floats; zeroed before the launch).
 __global__ void k_permute_samples(const float2* __restrict__ f, const int32_t* __restrict__ sidx, int64_t M,
-                                  float2* __restrict__ fp) {
-  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < M; k += (int64_t)gridDim.x * blockDim.x)
-    fp[k] = f[sidx[k]];
+                                  float2* __restrict__ fp, uint32_t* __restrict__ fmax) {
+  float mx = 0.f;
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < M; k += (int64_t)gridDim.x * blockDim.x) {
+    const float2 v = f[sidx[k]];
+    fp[k] = v;
+    mx = fmaxf(mx, fmaxf(fabsf(v.x), fabsf(v.y)));
+  }
+  const uint32_t m = __reduce_max_sync(0xffffffffu, __float_as_uint(mx));
+  if ((threadIdx.x & 31) == 0 && m != 0u) atomicMax(fmax, m);
 }
 
 template <int W, int WIN>
@@ -157,11 +195,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spread_tc(const float2* __res
   constexpr int SH = off_bits(3);
   constexpr uint32_t MASK = (1u << SH) - 1u;
   constexpr int kBuildThreads = kTcBuilders * 32;
-  constexpr int kExpWarps = kTcBuilders - kTcN / 8;             // builders expanding w0 / w1
+  constexpr int kBWarps = kTcN / 16;                            // builders of B: 16 rows x 2 node groups each
+  constexpr int kExpWarps = kTcBuilders - kBWarps;              // builders expanding w0 / w1
   constexpr int kMaxMt = (kTcMaxT0 + W - 1) * E1 / 128 + 1;     // M-tiles at the largest E0
-  constexpr int kAIters = (kMaxMt * 16 + kTcBuilders - 1) / kTcBuilders;
+  constexpr int kAIters = (kMaxMt * 8 + kTcBuilders - 1) / kTcBuilders;  // pairs of row groups per warp
   static_assert(2 * E2 <= kTcN, "complex columns must fit the MMA N");
-  static_assert(kExpWarps >= 1 && kTcK == 16, "staging roles assume 16 nodes and 8 B-row warps");
+  static_assert(kExpWarps >= 1 && kTcK == 16, "staging roles assume 16 nodes and 4 B-row warps");
   extern __shared__ __align__(16) unsigned char smem[];
   const int E0 = tl.E[0];
   const TcLayout L = tc_layout(W, E0);
@@ -204,20 +243,22 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spread_tc(const float2* __res
   // buffer gb & 1.
   if (warp < kTcBuilders) {
     // ======================= builder warps =======================
-    const int ri = lane & 7, kg = lane >> 3;  // operand builds: row in group, node group of 4
+    const int ri = lane & 7, kg = (lane >> 3) & 1, rh = lane >> 4;  // row in group, node group of 8, row group
     const float* sfrac = reinterpret_cast<const float*>(bins.sfrac);
     const float2* fperm = reinterpret_cast<const float2*>(bins.fperm);
     const float norm = (float)geo.norm;
+    const float bscale = norm * tc_scale_b(bins, norm);  // w2 f -> B
     const float mf = (float)geo.m;
     const TapK k0 = tap_k<WIN>(geo, 0), k1 = tap_k<WIN>(geo, 1), k2 = tap_k<WIN>(geo, 2);
-    // this thread's A rows (row groups warp + kTcBuilders i): offsets into wx, -1 past the tile
+    // this thread's A rows (row groups 2 (warp + kTcBuilders i) + rh): offsets into wx,
+    // -1 past the tile
     int a_off0[kAIters], a_off1[kAIters];
 #pragma unroll
     for (int i = 0; i < kAIters; ++i) {
-      const int r = (warp + kTcBuilders * i) * 8 + ri;
+      const int r = (2 * (warp + kTcBuilders * i) + rh) * 8 + ri;
       const int p0 = r / E1, p1 = r - p0 * E1;
-      a_off0[i] = r < rows ? p0 * kTcWxStride + kg * 4 : -1;
-      a_off1[i] = (E0 + p1) * kTcWxStride + kg * 4;
+      a_off0[i] = r < rows ? p0 * kTcWxStride + kg * 8 : -1;
+      a_off1[i] = (E0 + p1) * kTcWxStride + kg * 8;
     }
     // loads of one batch's records into ring slot `slot` (threads < 4 kTcK): thread
     // j < kTcK the window start and sample of node j, thread kTcK + i fraction i
@@ -270,25 +311,25 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spread_tc(const float2* __res
       unsigned char* a_hi = stage;
       unsigned char* a_lo = stage + L.a_bytes;
       unsigned char* b_hi = stage + 2 * L.a_bytes;
-      unsigned char* b_lo = b_hi + kTcN * kTcK * 4;
-      // (1) warps 0..7: B rows 8 w .. 8 w + 7; the other builders: w0 and w1 over planes and rows
-      if (warp < kTcN / 8) {
-        const int n = warp * 8 + ri, p2 = n >> 1, part = n & 1;
-        float vv[4];
+      unsigned char* b_lo = b_hi + kTcN * kTcK * 2;
+      // (1) warps 0..3: B row groups 2 w, 2 w + 1; the other builders: w0 and w1 over planes and rows
+      if (warp < kBWarps) {
+        const int rg = 2 * warp + rh, n = rg * 8 + ri, p2 = n >> 1, part = n & 1;
+        float vv[8];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const int j = kg * 4 + u;
+        for (int u = 0; u < 8; ++u) {
+          const int j = kg * 8 + u;
           const float w2 = tc_tap<WIN>(frac[j * 3 + 2], mf, p2 - (int)(roff[j] >> (2 * SH)), W, k2);
           const float2 c = val[j];
-          vv[u] = w2 * norm * (part ? c.y : c.x);
+          vv[u] = w2 * bscale * (part ? c.y : c.x);
         }
-        float4 hi, lo;
-        tc_split4(make_float4(vv[0], vv[1], vv[2], vv[3]), hi, lo);
-        const uint32_t o = tc_elem_off(warp, ri, kg);
-        *reinterpret_cast<float4*>(b_hi + o) = hi;
-        *reinterpret_cast<float4*>(b_lo + o) = lo;
+        uint4 hi, lo;
+        tc_split8_f16(vv, hi, lo);
+        const uint32_t o = tc_elem_off(rg, ri, kg);
+        *reinterpret_cast<uint4*>(b_hi + o) = hi;
+        *reinterpret_cast<uint4*>(b_lo + o) = lo;
       } else {
-        for (int i = tid - (kTcN / 8) * 32; i < (E0 + E1) * kTcK; i += kExpWarps * 32) {
+        for (int i = tid - kBWarps * 32; i < (E0 + E1) * kTcK; i += kExpWarps * 32) {
           const int j = i & (kTcK - 1), p = i / kTcK;
           const uint32_t off = roff[j];
           wx[p * kTcWxStride + j] = p < E0 ? tc_tap<WIN>(frac[j * 3 + 0], mf, p - (int)(off & MASK), W, k0)
@@ -297,22 +338,30 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spread_tc(const float2* __res
       }
       cp_async_wait_group<kTcAhead - 1>();  // this thread's loads of batch gb + 1 have landed
       tc::named_sync(1, kBuildThreads);     // (1) done; w0 / w1 and batch gb + 1's records visible
-      // (2) A: builder w takes row groups w, w + kTcBuilders, ...; rows past E0 E1 are zero
+      // (2) A: builder w takes row groups 2 w, 2 w + 1, then 2 (w + kTcBuilders), ...;
+      // rows past E0 E1 are zero
 #pragma unroll
       for (int i = 0; i < kAIters; ++i) {
-        const int rg = warp + kTcBuilders * i;
+        const int rg = 2 * (warp + kTcBuilders * i) + rh;
         if (rg < L.mt * 16) {
-          float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+          float v[8];
+#pragma unroll
+          for (int u = 0; u < 8; ++u) v[u] = 0.f;
           if (a_off0[i] >= 0) {
-            const float4 a = *reinterpret_cast<const float4*>(wx + a_off0[i]);
-            const float4 c = *reinterpret_cast<const float4*>(wx + a_off1[i]);
-            v = make_float4(a.x * c.x, a.y * c.y, a.z * c.z, a.w * c.w);
+            const float4 a0 = *reinterpret_cast<const float4*>(wx + a_off0[i]);
+            const float4 a1 = *reinterpret_cast<const float4*>(wx + a_off0[i] + 4);
+            const float4 c0 = *reinterpret_cast<const float4*>(wx + a_off1[i]);
+            const float4 c1 = *reinterpret_cast<const float4*>(wx + a_off1[i] + 4);
+            v[0] = a0.x * c0.x * kTcScaleA; v[1] = a0.y * c0.y * kTcScaleA;
+            v[2] = a0.z * c0.z * kTcScaleA; v[3] = a0.w * c0.w * kTcScaleA;
+            v[4] = a1.x * c1.x * kTcScaleA; v[5] = a1.y * c1.y * kTcScaleA;
+            v[6] = a1.z * c1.z * kTcScaleA; v[7] = a1.w * c1.w * kTcScaleA;
           }
-          float4 hi, lo;
-          tc_split4(v, hi, lo);
+          uint4 hi, lo;
+          tc_split8_f16(v, hi, lo);
           const uint32_t o = tc_elem_off(rg, ri, kg);
-          *reinterpret_cast<float4*>(a_hi + o) = hi;
-          *reinterpret_cast<float4*>(a_lo + o) = lo;
+          *reinterpret_cast<uint4*>(a_hi + o) = hi;
+          *reinterpret_cast<uint4*>(a_lo + o) = lo;
         }
       }
       tc::fence_proxy_async_smem();  // generic-proxy operand writes -> tensor core
@@ -330,9 +379,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spread_tc(const float2* __res
       const uint64_t d_ah = tc::smem_desc(sa0, kTcLBO, kTcSBO);
       const uint64_t d_al = tc::smem_desc(sa0 + L.a_bytes, kTcLBO, kTcSBO);
       const uint64_t d_bh = tc::smem_desc(sb0, kTcLBO, kTcSBO);
-      const uint64_t d_bl = tc::smem_desc(sb0 + kTcN * kTcK * 4, kTcLBO, kTcSBO);
+      const uint64_t d_bl = tc::smem_desc(sb0 + kTcN * kTcK * 2, kTcLBO, kTcSBO);
       const uint64_t d_stage = (uint64_t)(L.stage_bytes >> 4);  // stage s = stage 0 + s d_stage
-      const uint32_t idesc = tc::idesc_tf32(128, kTcN);
+      const uint32_t idesc = tc::idesc_f16(128, kTcN);
       uint32_t gb = 0, st = 0, cyc = 0, k = 0;
       int4 nxt = (int)blockIdx.x < num_items ? bins.items[blockIdx.x] : make_int4(0, 0, 0, 0);
       for (int it = blockIdx.x; it < num_items; it += G) {
@@ -351,13 +400,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spread_tc(const float2* __res
           for (int mt = 0; mt < L.mt; ++mt) {
             const uint32_t d = acc + (uint32_t)(mt * kTcN);
             const uint64_t am = so + (uint64_t)((mt * 16 * kTcSBO) >> 4);
-#pragma unroll
-            for (int ks = 0; ks < kTcK / 8; ++ks) {
-              const uint64_t ko = (uint64_t)((ks * 2 * kTcLBO) >> 4);
-              tc::mma_tf32(d, d_ah + am + ko, d_bh + so + ko, idesc, (b > 0 || ks > 0) ? 1u : 0u);
-              tc::mma_tf32(d, d_ah + am + ko, d_bl + so + ko, idesc, 1u);
-              tc::mma_tf32(d, d_al + am + ko, d_bh + so + ko, idesc, 1u);
-            }
+            tc::mma_f16(d, d_ah + am, d_bh + so, idesc, b > 0 ? 1u : 0u);  // K = 16: the whole batch
+            tc::mma_f16(d, d_ah + am, d_bl + so, idesc, 1u);
+            tc::mma_f16(d, d_al + am, d_bh + so, idesc, 1u);
           }
           tc::mma_commit(&empty[st]);
           if (++st == ns) {
@@ -383,6 +428,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spread_tc(const float2* __res
     const int64_t n0 = geo.n[0], n1 = geo.n[1], n2 = geo.n[2];
     const int E1a = tl.E[1], E2a = tl.E[2];
     const bool one_wrap = n2 >= E2a;
+    const float unscale = 1.f / (kTcScaleA * tc_scale_b(bins, (float)geo.norm));  // a power of two: exact
     uint32_t k = 0;
     int4 nxt = (int)blockIdx.x < num_items ? bins.items[blockIdx.x] : make_int4(0, 0, 0, 0);
     for (int it = blockIdx.x; it < num_items; it += G) {
@@ -416,7 +462,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spread_tc(const float2* __res
               const int p2 = c * 8 + 2 * u;  // pair (p2, p2 + 1): columns 4u .. 4u + 3 of this load
               if (p2 < E2a) {
                 float2* dst = one_wrap ? (p2 >= kw ? roww : rowa) + p2 : gi + rbase + wrap_up(o.a[2] + p2, n2);
-                const float4 w = make_float4(v[4 * u], v[4 * u + 1], v[4 * u + 2], v[4 * u + 3]);
+                const float4 w = make_float4(v[4 * u] * unscale, v[4 * u + 1] * unscale, v[4 * u + 2] * unscale,
+                                             v[4 * u + 3] * unscale);
                 if (p2 + 1 < E2a && (n2 & 1) == 0) {  // even row length: the pair is 16-byte aligned
                   if (w.x != 0.f || w.y != 0.f || w.z != 0.f || w.w != 0.f)
                     atomicAdd(reinterpret_cast<float4*>(dst), w);

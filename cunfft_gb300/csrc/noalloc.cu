@@ -43,7 +43,8 @@ constexpr size_t kOffNumItems = na_align(kOffItems + sizeof(int4) * kNaMaxItems)
 constexpr size_t kOffWork = na_align(kOffNumItems + sizeof(int32_t));
 constexpr size_t kOffInstOff = na_align(kOffWork + 2 * sizeof(int32_t));
 constexpr size_t kOffStatus = na_align(kOffInstOff + 2 * sizeof(int32_t));
-constexpr size_t kNaBytes = na_align(kOffStatus + sizeof(int32_t));
+constexpr size_t kOffFmax = na_align(kOffStatus + sizeof(int32_t));
+constexpr size_t kNaBytes = na_align(kOffFmax + sizeof(uint32_t));
 
 }  // namespace
 
@@ -127,6 +128,7 @@ extern "C" int cunfft_x_spread_noalloc(int d, const int64_t* N, const int64_t* n
   B.work = reinterpret_cast<int32_t*>(base + kOffWork);
   B.inst_off = reinterpret_cast<int32_t*>(base + kOffInstOff);  // unused for one instance
   B.status = reinterpret_cast<int32_t*>(base + kOffStatus);
+  B.fmax = reinterpret_cast<uint32_t*>(base + kOffFmax);
   B.M = M;
   B.max_items = kNaMaxItems;
   B.valid = 1;

@@ -419,6 +419,7 @@ int plan_init(Plan* p, int d, const int64_t* N, const int64_t* n, int m, int pre
   CG_TRY(check_cuda(p, cudaMalloc(&p->bins.work, sizeof(int32_t) * 2), "cudaMalloc"));
   CG_TRY(check_cuda(p, cudaMalloc(&p->bins.num_items, sizeof(int32_t)), "cudaMalloc"));
   CG_TRY(check_cuda(p, cudaMalloc(&p->bins.status, sizeof(int32_t)), "cudaMalloc"));
+  CG_TRY(check_cuda(p, cudaMalloc(&p->bins.fmax, sizeof(uint32_t)), "cudaMalloc"));
   CG_TRY(check_cuda(p, cudaMemset(p->bins.status, 0, sizeof(int32_t)), "cudaMemset"));
   p->M_inst = (int64_t*)calloc((size_t)batch, sizeof(int64_t));
   CG_TRY(plan_choose_tiling(p, nullptr, 0));
@@ -440,6 +441,8 @@ void plan_release(Plan* p) {
   cudaFree(p->bins.work);
   cudaFree(p->bins.num_items);
   cudaFree(p->bins.status);
+  cudaFree(p->bins.fmax);
+  p->bins.fmax = nullptr;
   p->bins.inst_off = nullptr;
   p->bins.work = nullptr;
   p->bins.num_items = nullptr;
