@@ -127,6 +127,21 @@ __device__ __forceinline__ void tc_split8_f16(const float* v, uint4& hi, uint4& 
   lo = make_uint4(l[0], l[1], l[2], l[3]);
 }
 
+// 4 FP32 values -> FP16 hi (4 halves) and lo = fp16(v - hi) (4 halves)
+__device__ __forceinline__ void tc_split4_f16(const float* v, uint2& hi, uint2& lo) {
+  uint32_t h[2], l[2];
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const __half2 hh = __floats2half2_rn(v[2 * i], v[2 * i + 1]);
+    const float2 hf = __half22float2(hh);
+    const __half2 ll = __floats2half2_rn(v[2 * i] - hf.x, v[2 * i + 1] - hf.y);
+    h[i] = *reinterpret_cast<const uint32_t*>(&hh);
+    l[i] = *reinterpret_cast<const uint32_t*>(&ll);
+  }
+  hi = make_uint2(h[0], h[1]);
+  lo = make_uint2(l[0], l[1]);
+}
+
 // 2^(kTcLogB - e), 2^e >= the call's largest |w2 f norm| (w2 <= 1): the B scale
 __device__ __forceinline__ float tc_scale_b(const Bins& bins, float norm) {
   int e = 0;
@@ -195,12 +210,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spread_tc(const float2* __res
   constexpr int SH = off_bits(3);
   constexpr uint32_t MASK = (1u << SH) - 1u;
   constexpr int kBuildThreads = kTcBuilders * 32;
-  constexpr int kBWarps = kTcN / 16;                            // builders of B: 16 rows x 2 node groups each
+  constexpr int kBWarps = kTcN / 8;                             // builders of B: one 8-row group each
   constexpr int kExpWarps = kTcBuilders - kBWarps;              // builders expanding w0 / w1
   constexpr int kMaxMt = (kTcMaxT0 + W - 1) * E1 / 128 + 1;     // M-tiles at the largest E0
   constexpr int kAIters = (kMaxMt * 8 + kTcBuilders - 1) / kTcBuilders;  // pairs of row groups per warp
   static_assert(2 * E2 <= kTcN, "complex columns must fit the MMA N");
-  static_assert(kExpWarps >= 1 && kTcK == 16, "staging roles assume 16 nodes and 4 B-row warps");
+  static_assert(kExpWarps >= 1 && kTcK == 16, "staging roles assume 16 nodes and 8 B-row warps");
   extern __shared__ __align__(16) unsigned char smem[];
   const int E0 = tl.E[0];
   const TcLayout L = tc_layout(W, E0);
@@ -248,6 +263,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spread_tc(const float2* __res
     const float2* fperm = reinterpret_cast<const float2*>(bins.fperm);
     const float norm = (float)geo.norm;
     const float bscale = norm * tc_scale_b(bins, norm);  // w2 f -> B
+    const int rg_end = (rows + 7) / 8;                   // A row groups holding rows of the tile
     const float mf = (float)geo.m;
     const TapK k0 = tap_k<WIN>(geo, 0), k1 = tap_k<WIN>(geo, 1), k2 = tap_k<WIN>(geo, 2);
     // this thread's A rows (row groups 2 (warp + kTcBuilders i) + rh): offsets into wx,
@@ -290,6 +306,16 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spread_tc(const float2* __res
       }
       cp_async_commit();
     }
+    // A rows past the tile's E0 E1 (up to the M-tiles' 128 L.mt) stay zero: written
+    // once here, never by the per-batch builds (published by their proxy fences)
+    {
+      const int rg0 = (rows + 7) / 8, ngrp = L.mt * 16 - rg0;
+      for (int i = tid; i < (int)ns * 2 * ngrp * 16; i += kBuildThreads) {
+        const int chunk = i & 15, grp = (i >> 4) % ngrp, part = (i >> 4) / ngrp;  // part: stage x (hi, lo)
+        unsigned char* base = smem + (size_t)(part >> 1) * L.stage_bytes + (size_t)(part & 1) * L.a_bytes;
+        *reinterpret_cast<uint4*>(base + (size_t)(rg0 + grp) * kTcSBO + chunk * 16) = make_uint4(0u, 0u, 0u, 0u);
+      }
+    }
     cp_async_wait_group<kTcAhead - 1>();
     tc::named_sync(1, kBuildThreads);  // records of batch 0 visible
     uint32_t gb = 0, st = 0, cyc = 0;  // batch, its stage and cycle
@@ -312,22 +338,23 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spread_tc(const float2* __res
       unsigned char* a_lo = stage + L.a_bytes;
       unsigned char* b_hi = stage + 2 * L.a_bytes;
       unsigned char* b_lo = b_hi + kTcN * kTcK * 2;
-      // (1) warps 0..3: B row groups 2 w, 2 w + 1; the other builders: w0 and w1 over planes and rows
+      // (1) warps 0..7: B row group w (lane: row ri, nodes 4 q4 .. 4 q4 + 3); the other
+      // builders: w0 and w1 over planes and rows
       if (warp < kBWarps) {
-        const int rg = 2 * warp + rh, n = rg * 8 + ri, p2 = n >> 1, part = n & 1;
-        float vv[8];
+        const int q4 = lane >> 3, n = warp * 8 + ri, p2 = n >> 1, part = n & 1;
+        float vv[4];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
-          const int j = kg * 8 + u;
+        for (int u = 0; u < 4; ++u) {
+          const int j = q4 * 4 + u;
           const float w2 = tc_tap<WIN>(frac[j * 3 + 2], mf, p2 - (int)(roff[j] >> (2 * SH)), W, k2);
           const float2 c = val[j];
           vv[u] = w2 * bscale * (part ? c.y : c.x);
         }
-        uint4 hi, lo;
-        tc_split8_f16(vv, hi, lo);
-        const uint32_t o = tc_elem_off(rg, ri, kg);
-        *reinterpret_cast<uint4*>(b_hi + o) = hi;
-        *reinterpret_cast<uint4*>(b_lo + o) = lo;
+        uint2 hi, lo;
+        tc_split4_f16(vv, hi, lo);
+        const uint32_t o = tc_elem_off(warp, ri, q4 >> 1) + (uint32_t)(q4 & 1) * 8u;
+        *reinterpret_cast<uint2*>(b_hi + o) = hi;
+        *reinterpret_cast<uint2*>(b_lo + o) = lo;
       } else {
         for (int i = tid - kBWarps * 32; i < (E0 + E1) * kTcK; i += kExpWarps * 32) {
           const int j = i & (kTcK - 1), p = i / kTcK;
@@ -338,12 +365,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spread_tc(const float2* __res
       }
       cp_async_wait_group<kTcAhead - 1>();  // this thread's loads of batch gb + 1 have landed
       tc::named_sync(1, kBuildThreads);     // (1) done; w0 / w1 and batch gb + 1's records visible
-      // (2) A: builder w takes row groups 2 w, 2 w + 1, then 2 (w + kTcBuilders), ...;
-      // rows past E0 E1 are zero
+      // (2) A: builder w takes row groups 2 w, 2 w + 1, then 2 (w + kTcBuilders), ...,
+      // up to the last group holding a row of the tile
 #pragma unroll
       for (int i = 0; i < kAIters; ++i) {
         const int rg = 2 * (warp + kTcBuilders * i) + rh;
-        if (rg < L.mt * 16) {
+        if (rg < rg_end) {
           float v[8];
 #pragma unroll
           for (int u = 0; u < 8; ++u) v[u] = 0.f;
