@@ -1,5 +1,5 @@
 // grid_interp_tc.cu -- launcher of the tensor-core 3D FP32 interpolation: the split of
-// the grid into padded TF32 hi/lo planes, then the TMA-fed kernel.
+// the grid into padded, per-plane scaled FP16 hi/lo planes, then the TMA-fed kernel.
 #include <cudaTypedefs.h>
 
 #include <algorithm>
@@ -27,64 +27,79 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_tiled() {
   return fn;
 }
 
-// Split planes float [batch][4][P0][P1][P2s] and the 5-D map over them (dims P2s, P1,
-// P0, component, instance; box 32 floats x E1 rows x CH planes, 128-byte swizzle,
-// zero fill outside).  Box rows are 128 bytes (32 floats), the innermost box extent
-// the swizzle allows; rows are multiples of 16 bytes (P2s % 4 == 0).
+void interp_tc_release(Plan& p) {
+  cudaFree(p.it_split);
+  cudaFree(p.it_pinv);
+  cudaFree(p.it_pmax);
+  p.it_split = nullptr;
+  p.it_pinv = nullptr;
+  p.it_pmax = nullptr;
+  p.it_ready = false;
+}
+
+// Split planes half [batch][4][P0][P1][P2s], plane scales float [batch][P0], and the
+// 5-D map over the planes (dims P2s, P1, P0, component, instance; box 32 halves x E1
+// rows x CH planes, 64-byte swizzle, zero fill outside).  Box rows are 64 bytes (32
+// halves), the innermost box extent the swizzle allows; rows are multiples of 16
+// bytes (P2s % 8 == 0).
 cudaError_t interp_tc_prepare(Plan& p) {
   if (p.it_ready) return cudaSuccess;
   const ItSplit sd = it_split_dims(p.geo);
   const size_t comp = (size_t)(sd.P0 * sd.P1 * sd.P2s);
-  const size_t bytes = sizeof(float) * 4 * comp * (size_t)p.geo.batch;
+  const size_t bytes = sizeof(__half) * 4 * comp * (size_t)p.geo.batch;
   PFN_cuTensorMapEncodeTiled_v12000 enc = encode_tiled();
   if (!enc) return cudaErrorNotSupported;
   if (!p.it_split) {
     cudaError_t e = cudaMalloc(&p.it_split, bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&p.it_pinv, sizeof(float) * (size_t)(sd.P0 * p.geo.batch));
+    if (e == cudaSuccess) e = cudaMalloc(&p.it_pmax, sizeof(uint32_t) * (size_t)(p.geo.n[0] * p.geo.batch));
     if (e != cudaSuccess) {
-      p.it_split = nullptr;
+      interp_tc_release(p);
       return e;
     }
   }
   const int E1 = it_e1(p.geo.W), CH = it_ch(p.geo.W);
   const cuuint64_t dims[5] = {(cuuint64_t)sd.P2s, (cuuint64_t)sd.P1, (cuuint64_t)sd.P0, 4u, (cuuint64_t)p.geo.batch};
-  const cuuint64_t strides[4] = {(cuuint64_t)(sd.P2s * 4), (cuuint64_t)(sd.P2s * sd.P1 * 4),
-                                 (cuuint64_t)(comp * 4), (cuuint64_t)(4 * comp * 4)};
+  const cuuint64_t strides[4] = {(cuuint64_t)(sd.P2s * 2), (cuuint64_t)(sd.P2s * sd.P1 * 2),
+                                 (cuuint64_t)(comp * 2), (cuuint64_t)(4 * comp * 2)};
   const cuuint32_t box[5] = {(cuuint32_t)kItK, (cuuint32_t)E1, (cuuint32_t)CH, 1u, 1u};
   const cuuint32_t estr[5] = {1u, 1u, 1u, 1u, 1u};
-  const CUresult r = enc(&p.it_tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 5, p.it_split, dims, strides, box, estr,
-                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+  const CUresult r = enc(&p.it_tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 5, p.it_split, dims, strides, box, estr,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
   p.it_ready = true;
   return cudaSuccess;
 }
 
-void interp_tc_release(Plan& p) {
-  cudaFree(p.it_split);
-  p.it_split = nullptr;
-  p.it_ready = false;
-}
 
 template <int W>
 static cudaError_t launch_it(const Plan& p, const void* in, void* out, cudaStream_t st) {
   if (!interp_tc_supported(p) || !p.it_ready) return cudaErrorInvalidConfiguration;
   const ItSplit sd = it_split_dims(p.geo);
+  cudaError_t e = cudaMemsetAsync(p.it_pmax, 0, sizeof(uint32_t) * (size_t)(p.geo.n[0] * p.geo.batch), st);
+  if (e != cudaSuccess) return e;
+  const int64_t per_plane = p.geo.n[1] * p.geo.n[2] / 4;
+  const unsigned ysplit = (unsigned)std::max<int64_t>(1, std::min<int64_t>((per_plane + 255) / 256,
+                                                                          (int64_t)p.num_sms * 8 / p.geo.n[0] + 1));
+  k_plane_absmax<<<dim3((unsigned)(p.geo.n[0] * p.geo.batch), ysplit), 256, 0, st>>>((const float2*)in, p.it_pmax,
+                                                                                    p.geo);
   const int64_t quads = sd.P0 * sd.P1 * (sd.P2s / 4) * p.geo.batch;
   const int sblocks = (int)std::min<int64_t>((quads + 255) / 256, (int64_t)p.num_sms * 16);
-  k_split_pad<<<sblocks, 256, 0, st>>>((const float2*)in, p.it_split, p.geo, sd);
+  k_split_pad<<<sblocks, 256, 0, st>>>((const float2*)in, p.it_pmax, (__half*)p.it_split, p.it_pinv, p.geo, sd);
   // 512 tensor-memory columns per CTA: at most one CTA per SM (more than half the
   // SM's 228 KB of shared memory), so tcgen05.alloc never waits
   const ItLayout L = it_layout();
   const size_t smem = L.dyn;
   static_assert(it_layout().dyn > 116u * 1024u, "one CTA per SM");
   auto kern = p.geo.window == kWinES ? k_interp_tc<W, kWinES> : k_interp_tc<W, kWinGauss>;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int per_sm = 0;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kItThreads, smem);
   if (e != cudaSuccess) return e;
   if (per_sm != 1) return cudaErrorInvalidConfiguration;
-  kern<<<p.num_sms, kItThreads, smem, st>>>(p.it_tmap, (float2*)out, p.geo, p.tl, p.bins);
+  kern<<<p.num_sms, kItThreads, smem, st>>>(p.it_tmap, p.it_pinv, (float2*)out, p.geo, p.tl, p.bins);
   return cudaGetLastError();
 }
 

@@ -1,4 +1,4 @@
-// kernels_interp_tc.cuh -- 3D FP32 interpolation on the tensor cores (tcgen05, 3xTF32),
+// kernels_interp_tc.cuh -- 3D FP32 interpolation on the tensor cores (tcgen05, 3 x FP16),
 // tile chunks streamed by TMA.
 //
 // Same work items, tiles and weights as k_interp (kernels_grid.cuh).  For a tile
@@ -14,19 +14,26 @@
 // the thread that owns node j finishes the w0 (x) w1 sum over its window from its own
 // lane, chunk by chunk, in registers.
 //
-// The grid is first split (k_split_pad) into TF32 hi + lo parts of its real and
-// imaginary parts, each a float array over the periodically padded index range
-// [0, n_t + W - 1) per dimension.  Every tile's padded box then lies inside those
+// Operands are FP16 hi + lo splits (11 + 11 significant bits, the precision of a TF32
+// split) multiplied as hi*hi + hi*lo + lo*hi with FP32 accumulation, K = 16 per MMA.
+// FP16's range is kept by exact powers of two: A (weights in [0, 1]) by 2^10, each
+// padded plane p0 of the grid by 2^(14 - e_p0), 2^e_p0 >= its largest |Re|, |Im|;
+// the node threads fold the inverse plane scales into their w0 weights.
+//
+// The grid is first split (k_plane_absmax, k_split_pad) into those FP16 hi + lo parts of its real and
+// imaginary parts, each an array over the periodically padded index range
+// [0, n_t + W - 1) per dimension.  Every tile's padded box then lies inside the
 // arrays (no wrap), and one thread loads each chunk with four TMA boxes (hi re, hi im,
-// lo re, lo im; 32 floats x E1 rows x CH planes) straight into the 128-byte swizzled
+// lo re, lo im; 32 halves x E1 rows x CH planes) straight into the 64-byte swizzled
 // K-major layout the MMAs read.  Warp roles: warp 0 lane 0 issues the TMA loads
-// (four chunk stages), warp 1 lane 0 the MMAs hi*hi + hi*lo + lo*hi per k-step of 8
-// columns, warps 2-5 (lane quarters) build A from their nodes' taps and reduce D.
-// Hand-offs are mbarriers (the chunk stages' with TMA transaction counts); every wait
-// is bounded and a wait that gives up sets the plan's device status flag.
+// (eight chunk stages), warp 1 lane 0 the MMAs, warps 2-9 (two per lane quarter) build
+// A from their nodes' taps and reduce D.  Hand-offs are mbarriers (the chunk stages'
+// with TMA transaction counts); every wait is bounded and a wait that gives up sets
+// the plan's device status flag.
 #pragma once
 
 #include <cuda.h>
+#include <cuda_fp16.h>
 
 #include "kernels_grid.cuh"
 #include "tc_sm100.cuh"
@@ -34,46 +41,63 @@
 namespace cg {
 
 constexpr int kItMaxT0 = 16;       // outer tile extent limit (E0 <= 31 planes)
-constexpr int kItK = 32;           // K: innermost tile columns p2 (E2 <= 31), padded; one 128-byte row
+constexpr int kItK = 32;           // K: innermost tile columns p2 (E2 <= 31), padded; one 64-byte row
 constexpr int kItNodes = 128;      // nodes per batch (MMA M)
 constexpr int kItTmaWarp = 0;
 constexpr int kItMmaWarp = 1;
-constexpr int kItNodeWarp0 = 2;    // 4 node warps: lane quarter = warp % 4
-constexpr int kItThreads = 6 * 32;
-constexpr uint32_t kItLBO = 128;               // A: core matrices along K
-constexpr uint32_t kItSBOA = 1024;             // A: 8-row groups (32 K values = 8 core matrices)
+constexpr int kItNodeWarp0 = 2;    // 8 node warps: lane quarter = warp % 4, pair half = (warp - 2) / 4
+constexpr int kItNodeWarps = 8;
+constexpr int kItThreads = (2 + kItNodeWarps) * 32;
 constexpr int kItHalf = 64;                    // B rows per part: real parts 0..63, imaginary 64..127
 constexpr int kItN = 2 * kItHalf;              // MMA N
-constexpr int kItStages = 4;                   // chunk stages = tensor-memory accumulators (kItN columns each)
-constexpr uint32_t kItPart = kItHalf * 128;    // one B part (hi re, hi im, lo re, lo im): 64 rows x 128 bytes
+constexpr int kItStages = 8;                   // chunk stages (TMA ring)
+constexpr int kItAcc = 4;                      // tensor-memory accumulators of kItN columns
+constexpr uint32_t kItLBO = 128;               // A: core matrices (8 rows x 8 halves) along K
+constexpr uint32_t kItSBOA = 512;              // A: 8-row groups (32 K values = 4 core matrices)
+constexpr uint32_t kItAPart = 128u * 64u;      // one A part (hi or lo): 128 rows x 64 bytes
+constexpr uint32_t kItPart = kItHalf * 64;     // one B part (hi re, hi im, lo re, lo im): 64 rows x 64 bytes
 constexpr uint32_t kItStage = 4 * kItPart;     // one chunk stage: B hi = parts 0-1, B lo = parts 2-3
+constexpr float kItScaleA = 1024.f;            // A = w2 in [0, 1] -> [0, 2^10]
+constexpr int kItWtStride = 55;                // floats per node in the weight table (odd: no bank conflicts)
+constexpr int kItLogB = 14;                    // |B| scaled to below 2^14 per plane
 constexpr uint32_t kItPolls = 1u << 20;        // mbarrier polls (<= 1 us each) before giving up
 
 __host__ __device__ constexpr int it_e1(int W) { return fixed_t_mid(3, W) + W - 1; }
 __host__ __device__ constexpr int it_ch(int W) { return kItHalf / it_e1(W); }                 // planes per chunk
 __host__ __device__ constexpr int it_pairs(int W) { return it_ch(W) * it_e1(W); }            // (plane, row) pairs <= 64
 
+// The innermost tile extent (a power of two <= 16, at most n2) must give TMA boxes a
+// 16-byte aligned start: at least 8 halves.
 __host__ __device__ constexpr bool interp_tc_ok(int d, int W, int T0, int64_t n2) {
-  return d == 3 && W >= 4 && W <= 16 && T0 >= 1 && T0 <= kItMaxT0 && n2 >= 4 && n2 % 4 == 0;
+  return d == 3 && W >= 4 && W <= 16 && T0 >= 1 && T0 <= kItMaxT0 && n2 >= 8 && n2 % 8 == 0;
 }
 
 // Shared-memory layout (byte offsets from a 1024-byte aligned base; host and device agree).
 struct ItLayout {
   uint32_t b_off;      // kItStages chunk stages of kItStage
-  uint32_t a_off;      // 2 buffers x (A hi, A lo), 16 KB each
-  uint32_t bar_off;    // afull[2], bfull[4], bempty[4], tfull[4], tempty[4]; tensor-memory base
+  uint32_t a_off;      // 2 buffers x (A hi, A lo)
+  uint32_t bar_off;    // afull[2], bfull[8], bempty[8], tfull[4], tempty[4]; tensor-memory base
+  uint32_t red_off;    // 2 x 128 float2: the second pair half's partial sums per node
+  uint32_t wt_off;     // [128][kItWtStride] floats: each node's w0 (planes) and w1 (rows) of the batch
   uint32_t total;      // bytes past the aligned base
   uint32_t dyn;        // dynamic shared memory to request (alignment slack included)
 };
 
 __host__ __device__ constexpr ItLayout it_layout() {
-  return ItLayout{0u, kItStages * kItStage, kItStages * kItStage + 4u * 16384u,
-                  kItStages * kItStage + 4u * 16384u + 160u, kItStages * kItStage + 4u * 16384u + 160u + 1024u};
+  return ItLayout{0u,
+                  kItStages * kItStage,
+                  kItStages * kItStage + 4u * kItAPart,
+                  kItStages * kItStage + 4u * kItAPart + 256u,
+                  kItStages * kItStage + 4u * kItAPart + 256u + 2048u,
+                  kItStages * kItStage + 4u * kItAPart + 256u + 2048u + 128u * kItWtStride * 4u,
+                  kItStages * kItStage + 4u * kItAPart + 256u + 2048u + 128u * kItWtStride * 4u + 1024u};
 }
 
-// Padded split planes of the grid: float [batch][4][P0][P1][P2s], component 0 hi re,
+// Padded split planes of the grid: half [batch][4][P0][P1][P2s], component 0 hi re,
 // 1 hi im, 2 lo re, 3 lo im; P_t = n_t + W - 1 holds grid index i mod n_t, P2s = P2
-// rounded up to a multiple of 4 (16-byte rows).
+// rounded up to a multiple of 8 (16-byte rows).  Plane scales: float [batch][P0],
+// the inverse 2^(e - 14) of each padded plane's scale, 2^e above the largest |Re|,
+// |Im| of its grid plane (uint32 [batch][n0] maxima, float bits).
 struct ItSplit {
   int64_t P0, P1, P2, P2s;
 };
@@ -82,31 +106,68 @@ __host__ __device__ inline ItSplit it_split_dims(const Geom& g) {
   s.P0 = g.n[0] + g.W - 1;
   s.P1 = g.n[1] + g.W - 1;
   s.P2 = g.n[2] + g.W - 1;
-  s.P2s = (s.P2 + 3) / 4 * 4;
+  s.P2s = (s.P2 + 7) / 8 * 8;
   return s;
 }
 
-// One thread per 4 consecutive p2 of one padded row: the quad never straddles the grid's
-// wrap (n2 % 4 == 0), reads two float4 of complex data and writes one float4 to each of
-// the four components.
-__global__ void k_split_pad(const float2* __restrict__ g, float* __restrict__ out, Geom geo, ItSplit sd) {
+// 4 FP32 values -> FP16 hi and lo = fp16(v - hi), 4 halves each
+__device__ __forceinline__ void it_split4_f16(float4 v, uint2& hi, uint2& lo) {
+  const __half2 h0 = __floats2half2_rn(v.x, v.y), h1 = __floats2half2_rn(v.z, v.w);
+  const float2 f0 = __half22float2(h0), f1 = __half22float2(h1);
+  const __half2 l0 = __floats2half2_rn(v.x - f0.x, v.y - f0.y), l1 = __floats2half2_rn(v.z - f1.x, v.w - f1.y);
+  hi = make_uint2(*reinterpret_cast<const uint32_t*>(&h0), *reinterpret_cast<const uint32_t*>(&h1));
+  lo = make_uint2(*reinterpret_cast<const uint32_t*>(&l0), *reinterpret_cast<const uint32_t*>(&l1));
+}
+
+// Largest |Re|, |Im| of every grid plane (instance, i0 < n0) into pmax (float bits,
+// zeroed before the launch): blockIdx.y runs over the plane's quads, blockIdx.x over
+// the planes; one atomic per warp.
+__global__ void k_plane_absmax(const float2* __restrict__ g, uint32_t* __restrict__ pmax, Geom geo) {
+  const int64_t plane = blockIdx.x, per = geo.n[1] * geo.n[2] / 4;
+  const float4* src = reinterpret_cast<const float4*>(g + plane * geo.n[1] * geo.n[2]);
+  float mx = 0.f;
+  for (int64_t e = blockIdx.y * (int64_t)blockDim.x + threadIdx.x; e < per; e += (int64_t)gridDim.y * blockDim.x) {
+    const float4 a = src[2 * e], b = src[2 * e + 1];
+    mx = fmaxf(mx, fmaxf(fmaxf(fmaxf(fabsf(a.x), fabsf(a.y)), fmaxf(fabsf(a.z), fabsf(a.w))),
+                         fmaxf(fmaxf(fabsf(b.x), fabsf(b.y)), fmaxf(fabsf(b.z), fabsf(b.w)))));
+  }
+  const uint32_t m = __reduce_max_sync(0xffffffffu, __float_as_uint(mx));
+  if ((threadIdx.x & 31) == 0 && m != 0u) atomicMax(pmax + plane, m);
+}
+
+// 2^(14 - e) with 2^e > mx, as the exponent e
+__device__ __forceinline__ int it_plane_exp(uint32_t mx_bits) {
+  int ex = 0;
+  frexpf(__uint_as_float(mx_bits), &ex);
+  return ex;
+}
+
+// One thread per 4 consecutive p2 of one padded row, a quad that never straddles the
+// grid's wrap (n2 % 8 == 0): FP16 hi + lo parts of the real and imaginary parts
+// scaled by the plane's 2^(14 - e); the thread of a plane's first quad also writes the
+// plane's inverse scale.
+__global__ void k_split_pad(const float2* __restrict__ g, const uint32_t* __restrict__ pmax, __half* __restrict__ out,
+                            float* __restrict__ inv_scale, Geom geo, ItSplit sd) {
   const int64_t q4 = sd.P2s / 4, row_q = sd.P1 * q4, per = sd.P0 * row_q, total = per * geo.batch;
   const int64_t comp = sd.P0 * sd.P1 * sd.P2s;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t inst = e / per, r = e - inst * per;
     const int64_t i0 = r / row_q, r2 = r - i0 * row_q;
     const int64_t i1 = r2 / q4, i2 = (r2 - i1 * q4) * 4;
-    const float2* src = g + inst * geo.ntot +
-                        (wrap_up(i0, geo.n[0]) * geo.n[1] + wrap_up(i1, geo.n[1])) * geo.n[2] + wrap_up(i2, geo.n[2]);
+    const int64_t gp = inst * geo.n[0] + wrap_up(i0, geo.n[0]);  // grid plane
+    const int ex = it_plane_exp(pmax[gp]);
+    const float scale = ldexpf(1.f, kItLogB - ex);
+    if (r2 == 0) inv_scale[inst * sd.P0 + i0] = ldexpf(1.f, ex - kItLogB);
+    const float2* src = g + gp * geo.n[1] * geo.n[2] + wrap_up(i1, geo.n[1]) * geo.n[2] + wrap_up(i2, geo.n[2]);
     const float4 a = reinterpret_cast<const float4*>(src)[0], b = reinterpret_cast<const float4*>(src)[1];
-    float4 h, l;
-    float* o = out + inst * 4 * comp + (i0 * sd.P1 + i1) * sd.P2s + i2;
-    tc_split4(make_float4(a.x, a.z, b.x, b.z), h, l);
-    *reinterpret_cast<float4*>(o) = h;
-    *reinterpret_cast<float4*>(o + 2 * comp) = l;
-    tc_split4(make_float4(a.y, a.w, b.y, b.w), h, l);
-    *reinterpret_cast<float4*>(o + comp) = h;
-    *reinterpret_cast<float4*>(o + 3 * comp) = l;
+    __half* o = out + inst * 4 * comp + (i0 * sd.P1 + i1) * sd.P2s + i2;
+    uint2 h, l;
+    it_split4_f16(make_float4(a.x * scale, a.z * scale, b.x * scale, b.z * scale), h, l);
+    *reinterpret_cast<uint2*>(o) = h;
+    *reinterpret_cast<uint2*>(o + 2 * comp) = l;
+    it_split4_f16(make_float4(a.y * scale, a.w * scale, b.y * scale, b.w * scale), h, l);
+    *reinterpret_cast<uint2*>(o + comp) = h;
+    *reinterpret_cast<uint2*>(o + 3 * comp) = l;
   }
 }
 
@@ -157,6 +218,7 @@ __device__ __forceinline__ ItRec it_load_rec(const ItCursor& c, int num_items, i
 
 template <int W, int WIN>
 __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const __grid_constant__ CUtensorMap tmap,
+                                                             const float* __restrict__ plane_inv,
                                                              float2* __restrict__ f, Geom geo, Tiling tl, Bins bins) {
   constexpr int E1 = it_e1(W), CH = it_ch(W), NP = it_pairs(W);
   constexpr int E0MAX = kItMaxT0 + W - 1;
@@ -164,19 +226,20 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const __grid_consta
   constexpr int GI = (NP + 15) / 16;  // 16-pair groups of the tensor-memory read-out
   constexpr int SH = off_bits(3);
   constexpr uint32_t MASK = (1u << SH) - 1u;
-  constexpr uint32_t kBoxBytes = (uint32_t)(kItK * 4 * E1 * CH);
+  constexpr uint32_t kBoxBytes = (uint32_t)(kItK * 2 * E1 * CH);
   static_assert(NP <= kItHalf && NP > 0, "a chunk's (plane, row) pairs must fit one B part");
-  static_assert(kItStages * kItN <= 512, "the accumulators must fit tensor memory");
+  static_assert(kItAcc * kItN <= 512, "the accumulators must fit tensor memory");
   static_assert(fixed_t_last(3, W) + W - 1 <= kItK, "innermost padded extent must fit K");
+  static_assert(E0MAX + E1 <= kItWtStride, "a node's w0 and w1 must fit its weight-table row");
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = smem_raw + ((1024u - (tc::smem_u32(smem_raw) & 1023u)) & 1023u);
   const ItLayout L = it_layout();
   uint64_t* afull = reinterpret_cast<uint64_t*>(smem + L.bar_off);  // [2] A of the batch built
-  uint64_t* bfull = afull + 2;                                       // [4] tile chunk landed (TMA)
-  uint64_t* bempty = afull + 6;                                      // [4] MMAs of the chunk complete
-  uint64_t* tfull = afull + 10;                                      // [4] accumulator complete
-  uint64_t* tempty = afull + 14;                                     // [4] accumulator read out
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + L.bar_off + 144);
+  uint64_t* bfull = afull + 2;                                       // [8] tile chunk landed (TMA)
+  uint64_t* bempty = afull + 2 + kItStages;                          // [8] MMAs of the chunk complete
+  uint64_t* tfull = afull + 2 + 2 * kItStages;                       // [4] accumulator complete
+  uint64_t* tempty = tfull + kItAcc;                                 // [4] accumulator read out
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tempty + kItAcc);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int E0 = tl.E[0];
   const int nch = (E0 + CH - 1) / CH;
@@ -184,12 +247,14 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const __grid_consta
   const int G = (int)gridDim.x;
 
   if (tid == 0) {
-    for (int i = 0; i < 2; ++i) tc::mbar_init(&afull[i], 4);  // one arrival per node warp
+    for (int i = 0; i < 2; ++i) tc::mbar_init(&afull[i], kItNodeWarps);  // one arrival per node warp
     for (int i = 0; i < kItStages; ++i) {
       tc::mbar_init(&bfull[i], 1);    // the TMA thread's arrival (+ the boxes' bytes)
       tc::mbar_init(&bempty[i], 1);
+    }
+    for (int i = 0; i < kItAcc; ++i) {
       tc::mbar_init(&tfull[i], 1);
-      tc::mbar_init(&tempty[i], 4);   // one arrival per node warp
+      tc::mbar_init(&tempty[i], kItNodeWarps);  // one arrival per node warp
     }
     tc::mbar_fence_init();
   }
@@ -205,7 +270,8 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const __grid_consta
 
   // Every role walks items c, c + G, ... (CTA c), batches of 128 nodes within an
   // item and nch chunks within a batch; chunk gc (counted across the CTA's whole
-  // sequence) uses chunk stage and accumulator gc & 3 in their cycle gc >> 2.
+  // sequence) uses chunk stage gc & 7 in its cycle gc >> 3 and accumulator gc & 3
+  // in its cycle gc >> 2.
   if (warp == kItTmaWarp) {
     // ======================= TMA: tile chunks =======================
     if (lane == 0) {
@@ -216,11 +282,12 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const __grid_consta
         const int nbatch = (item.z - item.y + kItNodes - 1) / kItNodes;
         for (int bt = 0; bt < nbatch; ++bt) {
           for (int c = 0; c < nch; ++c, ++gc) {
-            const uint32_t buf = gc & 3u;
-            if (gc >= 4) healthy &= tc::mbar_wait_bounded(&bempty[buf], ((gc >> 2) - 1u) & 1u, kItPolls);
+            const uint32_t buf = gc % kItStages;
+            if (gc >= kItStages)
+              healthy &= tc::mbar_wait_bounded(&bempty[buf], ((gc / kItStages) - 1u) & 1u, kItPolls);
             unsigned char* st = smem + L.b_off + buf * kItStage;
             tc::mbar_arrive_expect_tx(&bfull[buf], 4u * kBoxBytes);
-            // x = o.a[2] is a multiple of the innermost tile extent (>= 4 floats: 16 bytes)
+            // x = o.a[2] is a multiple of the innermost tile extent (>= 8 halves: 16 bytes)
             for (int comp = 0; comp < 4; ++comp)
               tc::tma_load_5d(st + comp * kItPart, &tmap, (int)o.a[2], (int)o.a[1], (int)o.a[0] + c * CH, comp,
                               (int)o.inst, &bfull[buf]);
@@ -229,20 +296,20 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const __grid_consta
       }
       // the boxes of the last chunks have landed before this CTA can exit
       for (uint32_t k = 1; k <= (uint32_t)kItStages && k <= gc; ++k)
-        healthy &= tc::mbar_wait_bounded(&bfull[(gc - k) & 3u], ((gc - k) >> 2) & 1u, kItPolls);
+        healthy &= tc::mbar_wait_bounded(&bfull[(gc - k) % kItStages], ((gc - k) / kItStages) & 1u, kItPolls);
     }
     __syncwarp();
   } else if (warp == kItMmaWarp) {
     // ======================= MMA issuer: lane 0 =======================
     if (lane == 0) {
       const uint32_t sa = tc::smem_u32(smem + L.a_off), sb = tc::smem_u32(smem + L.b_off);
-      const uint64_t d_abuf = (uint64_t)(32768u >> 4);  // A buffer 1 = buffer 0 + d_abuf
+      const uint64_t d_abuf = (uint64_t)((2u * kItAPart) >> 4);  // A buffer 1 = buffer 0 + d_abuf
       const uint64_t d_ah = tc::smem_desc(sa, kItLBO, kItSBOA);
-      const uint64_t d_al = tc::smem_desc(sa + 16384u, kItLBO, kItSBOA);
-      const uint64_t d_bh = tc::smem_desc_sw128(sb);
-      const uint64_t d_bl = tc::smem_desc_sw128(sb + 2u * kItPart);
+      const uint64_t d_al = tc::smem_desc(sa + kItAPart, kItLBO, kItSBOA);
+      const uint64_t d_bh = tc::smem_desc_sw64(sb);
+      const uint64_t d_bl = tc::smem_desc_sw64(sb + 2u * kItPart);
       const uint64_t d_buf = (uint64_t)(kItStage >> 4);  // stage k = stage 0 + k d_buf
-      const uint32_t idesc = tc::idesc_tf32(128, kItN);
+      const uint32_t idesc = tc::idesc_f16(128, kItN);
       uint32_t gc = 0, gbt = 0;
       for (int it = blockIdx.x; it < num_items; it += G) {
         const int4 item = bins.items[it];
@@ -252,56 +319,63 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const __grid_consta
           healthy &= tc::mbar_wait_bounded(&afull[ab], (gbt >> 1) & 1u, kItPolls);
           const uint64_t ao = ab ? d_abuf : 0ull;
           for (int c = 0; c < nch; ++c, ++gc) {
-            const uint32_t buf = gc & 3u;
-            healthy &= tc::mbar_wait_bounded(&bfull[buf], (gc >> 2) & 1u, kItPolls);
-            if (gc >= 4) healthy &= tc::mbar_wait_bounded(&tempty[buf], ((gc >> 2) - 1u) & 1u, kItPolls);
+            const uint32_t buf = gc % kItStages, acc = gc % kItAcc;
+            healthy &= tc::mbar_wait_bounded(&bfull[buf], (gc / kItStages) & 1u, kItPolls);
+            if (gc >= kItAcc) healthy &= tc::mbar_wait_bounded(&tempty[acc], ((gc / kItAcc) - 1u) & 1u, kItPolls);
             tc::fence_after_sync();
-            const uint32_t d = tmem + buf * (uint32_t)kItN;
+            const uint32_t d = tmem + acc * (uint32_t)kItN;
             const uint64_t bo = (uint64_t)buf * d_buf;
 #pragma unroll
-            for (int ks = 0; ks < kItK / 8; ++ks) {
+            for (int ks = 0; ks < kItK / 16; ++ks) {
               const uint64_t ka = (uint64_t)((ks * 2 * kItLBO) >> 4);  // A: two core matrices per k-step
               const uint64_t kb = (uint64_t)((ks * 32) >> 4);          // B: 32 bytes into the swizzled row
-              tc::mma_tf32(d, d_ah + ao + ka, d_bh + bo + kb, idesc, ks > 0 ? 1u : 0u);
-              tc::mma_tf32(d, d_ah + ao + ka, d_bl + bo + kb, idesc, 1u);
-              tc::mma_tf32(d, d_al + ao + ka, d_bh + bo + kb, idesc, 1u);
+              tc::mma_f16(d, d_ah + ao + ka, d_bh + bo + kb, idesc, ks > 0 ? 1u : 0u);
+              tc::mma_f16(d, d_ah + ao + ka, d_bl + bo + kb, idesc, 1u);
+              tc::mma_f16(d, d_al + ao + ka, d_bh + bo + kb, idesc, 1u);
             }
             tc::mma_commit(&bempty[buf]);
-            tc::mma_commit(&tfull[buf]);
+            tc::mma_commit(&tfull[acc]);
           }
         }
       }
       // the last chunk commits are waited by the node warps; the last bempty arrivals here
       for (uint32_t k = 1; k <= (uint32_t)kItStages && k <= gc; ++k)
-        healthy &= tc::mbar_wait_bounded(&bempty[(gc - k) & 3u], ((gc - k) >> 2) & 1u, kItPolls);
+        healthy &= tc::mbar_wait_bounded(&bempty[(gc - k) % kItStages], ((gc - k) / kItStages) & 1u, kItPolls);
     }
     __syncwarp();
   } else {
     // ======================= node warps: A, then the w0 (x) w1 reduction =======================
+    // Two warps per tensor-memory lane quarter: half h builds A's K values 16 h .. 16 h + 15
+    // of its nodes and reduces the first (h = 0) or second (h = 1) half of each chunk's
+    // (plane, row) pairs; half 1 hands its sums over through shared memory once per batch.
     // Records are loaded two batches ahead; A of batch gbt + 1 is built at the start
     // of batch gbt (its buffer's previous batch, gbt - 1, is complete: this thread
     // waited for all of its accumulators), so the MMAs never wait for A.
+    constexpr int GI0 = (GI + 1) / 2;   // 16-pair groups of half 0
     const int q = warp & 3;             // tensor-memory lane quarter
+    const int h = (warp - kItNodeWarp0) >> 2;
     const int slot = 32 * q + lane;     // node slot in the batch = TMEM lane = A row
+    float2* red = reinterpret_cast<float2*>(smem + L.red_off);
     const float norm = (float)geo.norm;
     const float mf = (float)geo.m;
+    const int64_t P0 = it_split_dims(geo).P0;
     const TapK k0 = tap_k<WIN>(geo, 0), k1 = tap_k<WIN>(geo, 1), k2 = tap_k<WIN>(geo, 2);
     auto build_a = [&](const ItRec& r, uint32_t ab) {
-      unsigned char* ah = smem + L.a_off + ab * 32768u;
-      unsigned char* al = ah + 16384u;
+      unsigned char* ah = smem + L.a_off + ab * 2u * kItAPart;
+      unsigned char* al = ah + kItAPart;
       const int o2 = (int)(r.off >> (2 * SH));
 #pragma unroll
-      for (int k4 = 0; k4 < kItK / 4; ++k4) {
-        float4 v;
-        v.x = tc_tap<WIN>(r.fr2, mf, 4 * k4 + 0 - o2, W, k2);
-        v.y = tc_tap<WIN>(r.fr2, mf, 4 * k4 + 1 - o2, W, k2);
-        v.z = tc_tap<WIN>(r.fr2, mf, 4 * k4 + 2 - o2, W, k2);
-        v.w = tc_tap<WIN>(r.fr2, mf, 4 * k4 + 3 - o2, W, k2);
-        float4 h, l;
-        tc_split4(v, h, l);
-        const uint32_t oa = (uint32_t)(slot >> 3) * kItSBOA + (uint32_t)k4 * kItLBO + (uint32_t)(slot & 7) * 16u;
-        *reinterpret_cast<float4*>(ah + oa) = h;
-        *reinterpret_cast<float4*>(al + oa) = l;
+      for (int kk = 0; kk < kItK / 16; ++kk) {
+        const int k8 = 2 * h + kk;
+        float t[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) t[u] = tc_tap<WIN>(r.fr2, mf, 8 * k8 + u - o2, W, k2) * kItScaleA;
+        uint2 h0, l0, h1, l1;
+        it_split4_f16(make_float4(t[0], t[1], t[2], t[3]), h0, l0);
+        it_split4_f16(make_float4(t[4], t[5], t[6], t[7]), h1, l1);
+        const uint32_t oa = (uint32_t)(slot >> 3) * kItSBOA + (uint32_t)k8 * kItLBO + (uint32_t)(slot & 7) * 16u;
+        *reinterpret_cast<uint4*>(ah + oa) = make_uint4(h0.x, h0.y, h1.x, h1.y);
+        *reinterpret_cast<uint4*>(al + oa) = make_uint4(l0.x, l0.y, l1.x, l1.y);
       }
       tc::fence_proxy_async_smem();
       tc::mbar_arrive_warp(&afull[ab]);
@@ -315,49 +389,92 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const __grid_consta
     ItRec rc = it_load_rec(c0, num_items, slot, bins), rn = it_load_rec(c1, num_items, slot, bins);
     if (c0.it < num_items) build_a(rc, 0u);
     uint32_t gc = 0, gbt = 0;
+    float* wt = reinterpret_cast<float*>(smem + L.wt_off) + slot * kItWtStride;  // w0 [0, E0MAX), w1 after
     for (; c0.it < num_items; ++gbt) {
+      // this batch's plane scales (half 0): the loads go out before A of the next batch is built
+      const TileOrigin to = decode_tile<3>(geo, tl, c0.item.x);
+      const float* pinv = plane_inv + to.inst * P0 + to.a[0];
+      const int64_t pmax = P0 - to.a[0];  // padded planes left from the tile's first
+      float psc[E0MAX];
+      if (h == 0) {
+#pragma unroll
+        for (int p = 0; p < E0MAX; ++p) psc[p] = p < pmax ? pinv[p] : 0.f;
+      }
       if (c1.it < num_items) build_a(rn, (gbt + 1u) & 1u);
       const ItRec rnn = it_load_rec(c2, num_items, slot, bins);
-      const int o0 = (int)(rc.off & MASK), o1 = (int)((rc.off >> SH) & MASK);
-      // expanded w0 (planes) and w1 (rows) of this node
-      float w0x[E0MAX], w1x[E1];
+      // weight table: half 0 w0 over planes (times each plane's inverse scale and
+      // 2^-10), half 1 w1 over rows; the previous batch's readers are past its barrier
+      if (h == 0) {
+        const int o0 = (int)(rc.off & MASK);
 #pragma unroll
-      for (int p = 0; p < E0MAX; ++p) w0x[p] = tc_tap<WIN>(rc.fr0, mf, p - o0, W, k0);
+        for (int p = 0; p < E0MAX; ++p) wt[p] = tc_tap<WIN>(rc.fr0, mf, p - o0, W, k0) * (psc[p] * (1.f / kItScaleA));
+      } else {
+        const int o1 = (int)((rc.off >> SH) & MASK);
 #pragma unroll
-      for (int p = 0; p < E1; ++p) w1x[p] = tc_tap<WIN>(rc.fr1, mf, p - o1, W, k1);
+        for (int p = 0; p < E1; ++p) wt[E0MAX + p] = tc_tap<WIN>(rc.fr1, mf, p - o1, W, k1);
+      }
+      tc::named_sync(1, kItNodeWarps * 32);
+      float w1x[E1];
+#pragma unroll
+      for (int p = 0; p < E1; ++p) w1x[p] = wt[E0MAX + p];
       float accx = 0.f, accy = 0.f;
+#pragma unroll 1
+      for (int c = 0; c < nch; ++c) {
+        const uint32_t acc = gc % kItAcc;
+        healthy &= tc::mbar_wait_warp(&tfull[acc], (gc / kItAcc) & 1u, kItPolls);
+        tc::fence_after_sync();
+        const uint32_t t0 = tmem + ((uint32_t)(32 * q) << 16) + acc * (uint32_t)kItN;
+        // per plane of the chunk: sum over its rows of w1 times the column, then w0 once
+        float sx[CH], sy[CH];
 #pragma unroll
-      for (int c = 0; c < MAXCH; ++c) {
-        if (c < nch) {
-          const uint32_t buf = gc & 3u;
-          healthy &= tc::mbar_wait_warp(&tfull[buf], (gc >> 2) & 1u, kItPolls);
-          tc::fence_after_sync();
-          const uint32_t t0 = tmem + ((uint32_t)(32 * q) << 16) + buf * (uint32_t)kItN;
+        for (int pl = 0; pl < CH; ++pl) sx[pl] = sy[pl] = 0.f;
+        // this half's pair groups (warp-uniform): every load issued, then one wait
+        float vr[GI0][16], vi[GI0][16];
 #pragma unroll
-          for (int gi = 0; gi < GI; ++gi) {
-            float vr[16], vi[16];
-            tc::tmem_ld16(t0 + (uint32_t)(gi * 16), vr);         // real parts of pairs 16 gi ..
-            tc::tmem_ld16(t0 + (uint32_t)kItHalf + (uint32_t)(gi * 16), vi);  // imaginary parts
-            tc::tmem_ld_wait();
+        for (int gq = 0; gq < GI0; ++gq) {
+          const int gi = h * GI0 + gq;
+          if (gi < GI) {
+            tc::tmem_ld16(t0 + (uint32_t)(gi * 16), vr[gq]);                    // real parts of pairs 16 gi ..
+            tc::tmem_ld16(t0 + (uint32_t)kItHalf + (uint32_t)(gi * 16), vi[gq]);  // imaginary parts
+          }
+        }
+        tc::tmem_ld_wait();
+        tc::fence_before_sync();
+        tc::mbar_arrive_warp(&tempty[acc]);
 #pragma unroll
-            for (int u = 0; u < 16; ++u) {
-              const int pr = gi * 16 + u;  // (plane pl, row p1) of the chunk
-              if (pr < NP) {
-                const int pl = pr / E1, p1 = pr - (pr / E1) * E1;
-                if (c * CH + pl < E0MAX) {
-                  const float w = w0x[c * CH + pl] * w1x[p1];
-                  accx = fmaf(w, vr[u], accx);
-                  accy = fmaf(w, vi[u], accy);
-                }
-              }
+        for (int gi = 0; gi < GI; ++gi) {
+          if ((gi >= GI0 ? 1 : 0) != h) continue;
+          const int gq = gi - (gi >= GI0 ? GI0 : 0);
+#pragma unroll
+          for (int u = 0; u < 16; ++u) {
+            const int pr = gi * 16 + u;  // (plane pl, row p1) of the chunk
+            if (pr < NP) {
+              const int pl = pr / E1, p1 = pr - (pr / E1) * E1;
+              sx[pl] = fmaf(w1x[p1], vr[gq][u], sx[pl]);
+              sy[pl] = fmaf(w1x[p1], vi[gq][u], sy[pl]);
             }
           }
-          tc::fence_before_sync();
-          tc::mbar_arrive_warp(&tempty[buf]);
-          ++gc;
         }
+#pragma unroll
+        for (int pl = 0; pl < CH; ++pl) {
+          const int p0 = c * CH + pl;
+          if (p0 < E0MAX) {
+            const float w0 = wt[p0];
+            accx = fmaf(w0, sx[pl], accx);
+            accy = fmaf(w0, sy[pl], accy);
+          }
+        }
+        ++gc;
       }
-      if (rc.idx >= 0) f[rc.idx] = make_float2(accx * norm, accy * norm);
+      // half 1's sums to half 0 (buffer gbt & 1: half 0 read the other one before this
+      // batch's barrier), which writes the sample
+      float2* rb = red + (gbt & 1u) * 128u;
+      if (h == 1) rb[slot] = make_float2(accx, accy);
+      tc::named_sync(1, kItNodeWarps * 32);
+      if (h == 0) {
+        const float2 o = rb[slot];
+        if (rc.idx >= 0) f[rc.idx] = make_float2((accx + o.x) * norm, (accy + o.y) * norm);
+      }
       rc = rn;
       rn = rnn;
       c0 = c1;

@@ -62,9 +62,11 @@ struct Plan {
   uint64_t g_gen[2] = {0, 0};
   uint64_t node_gen = 0;  // bumped by every node binding / tiling change
   HostPath* hp = nullptr; // created by the first host-buffer transform
-  // tensor-core interpolation: the grid's padded TF32 hi/lo planes and their TMA map,
-  // created before its first launch (interp_tc_prepare)
-  float* it_split = nullptr;
+  // tensor-core interpolation: the grid's padded FP16 hi/lo planes, their per-plane
+  // inverse scales and their TMA map, created before its first launch (interp_tc_prepare)
+  void* it_split = nullptr;
+  float* it_pinv = nullptr;
+  uint32_t* it_pmax = nullptr;
   CUtensorMap it_tmap{};
   bool it_ready = false;
 };

@@ -36,6 +36,15 @@ __device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t saddr) {
          (2ull << 61);
 }
 
+// K-major operand in the 64-byte swizzled layout of a TMA load with
+// CU_TENSOR_MAP_SWIZZLE_64B: rows of 64 bytes (32 FP16 K values), 8-row atoms of
+// 512 bytes (SBO), layout type 4 (64-byte swizzle) in bits 61-63; atoms on 512-byte
+// boundaries, the k-th group of 16 K values 32 k bytes into the row.
+__device__ __forceinline__ uint64_t smem_desc_sw64(uint32_t saddr) {
+  return (uint64_t)((saddr & 0x3FFFFu) >> 4) | (1ull << 16) | ((uint64_t)(512u >> 4) << 32) | (1ull << 46) |
+         (4ull << 61);
+}
+
 // ---- instruction descriptor: kind::tf32, FP32 accumulator, A and B K-major ----
 __host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
   return (1u << 4)                        // D format: F32

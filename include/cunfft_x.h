@@ -70,7 +70,7 @@ typedef struct cunfft_x_plan cunfft_x_plan;
  *  src/cunfft.cu:296-299).  The reference wraps window indices with &(n-1)
  *  (src/cunfft_kernel.cu:590, :768, :1036), so there n must be a power of two;
  *  here any size wraps correctly.  The tensor-core gridding forms need 3D with an
- *  even last size (spreading) or one divisible by 4 (interpolation); other
+ *  even last size (spreading) or one divisible by 8 (interpolation); other
  *  sizes run the shared-tile forms.  1 <= m <= 15; precision CUNFFT_X_F64 or
  *  CUNFFT_X_F32; batch >= 1 instances; stream 0 creates a private stream
  *  (a cudaStream_t may be passed as void*). */

@@ -32,7 +32,7 @@ def _rand(shape, rng):
 CASES = [
     ([10], [24]), ([33], [70]), ([31], [45]),                  # 1D: even n, odd N, odd n
     ([12, 20], [24, 50]), ([15, 9], [30, 27]),                 # 2D: 50 = 2 x 25, odd N and odd n
-    ([12, 10, 20], [24, 30, 40]),                              # 3D, last size divisible by 4
+    ([12, 10, 20], [24, 30, 40]),                              # 3D, last size divisible by 8
     ([9, 11, 13], [18, 22, 26]),                               # 3D, last size even only
     ([10, 10, 11], [20, 21, 27]),                              # 3D, odd sizes
 ]
@@ -63,8 +63,8 @@ def test_general_sizes_match_oracle(dev, N, n, prec):
                                  ([10, 10, 11], [20, 21, 27])])
 def test_general_sizes_every_kernel_form(dev, N, n):
     """FP32 3D: each spreading and interpolation form the plan offers, on grids whose
-    last size is divisible by 4, only even, or odd (the tensor-core forms' 16-byte pairs
-    and quads need the even / divisible-by-4 row length)."""
+    last size is divisible by 8, only even, or odd (the tensor-core forms' 16-byte pairs
+    and boxes need the even / divisible-by-8 row length)."""
     from cunfft_gb300.nfft import NFFT
     rng = np.random.default_rng(sum(n))
     M = 5000
@@ -83,7 +83,7 @@ def test_general_sizes_every_kernel_form(dev, N, n):
     g = _rand(n, rng)
     gt = torch.from_numpy(g).to(dev).to(torch.complex64)
     ref_f = O.interp(x, g, N, n, 5)
-    kinds = ["tensor", "shared"] if n[2] % 4 == 0 else ["shared"]
+    kinds = ["tensor", "shared"] if n[2] % 8 == 0 else ["shared"]
     assert p.interp_kernel() == kinds[0]
     for k in kinds:
         p.set_interp_kernel(k)
