@@ -326,8 +326,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spread_tc(const float2* __res
         tc_cursor_step(lc, bins, num_items);
       }
       cp_async_commit();
-      // stage st is free once the MMAs of batch gb - ns (its previous cycle) are complete
-      if (cyc > 0) healthy &= tc::mbar_wait_bounded(&empty[st], (cyc - 1u) & 1u, kTcPolls);
+      // stage st is free once the MMAs of batch gb - ns (its previous cycle) are complete:
+      // one thread waits, and the builders' barrier after phase (1) publishes it (the
+      // stage is written only in phase (2); a wait by every thread would poll one
+      // mbarrier word from 32 lanes per warp)
+      if (cyc > 0 && tid == kBuildThreads - 32)
+        healthy &= tc::mbar_wait_bounded(&empty[st], (cyc - 1u) & 1u, kTcPolls);
       const unsigned char* sl = smem + L.rec_off + (gb % kTcRing) * kTcSlotBytes;
       const uint32_t* roff = reinterpret_cast<const uint32_t*>(sl + kTcSlotOff);
       const float* frac = reinterpret_cast<const float*>(sl + kTcSlotFrac);
@@ -338,11 +342,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spread_tc(const float2* __res
       unsigned char* a_lo = stage + L.a_bytes;
       unsigned char* b_hi = stage + 2 * L.a_bytes;
       unsigned char* b_lo = b_hi + kTcN * kTcK * 2;
-      // (1) warps 0..7: B row group w (lane: row ri, nodes 4 q4 .. 4 q4 + 3); the other
-      // builders: w0 and w1 over planes and rows
+      // (1) warps 0..7: B row group w (lane: row ri, nodes 4 q4 .. 4 q4 + 3) into registers;
+      // the other builders: w0 and w1 over planes and rows
+      float vv[4];
       if (warp < kBWarps) {
         const int q4 = lane >> 3, n = warp * 8 + ri, p2 = n >> 1, part = n & 1;
-        float vv[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
           const int j = q4 * 4 + u;
@@ -350,11 +354,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spread_tc(const float2* __res
           const float2 c = val[j];
           vv[u] = w2 * bscale * (part ? c.y : c.x);
         }
-        uint2 hi, lo;
-        tc_split4_f16(vv, hi, lo);
-        const uint32_t o = tc_elem_off(warp, ri, q4 >> 1) + (uint32_t)(q4 & 1) * 8u;
-        *reinterpret_cast<uint2*>(b_hi + o) = hi;
-        *reinterpret_cast<uint2*>(b_lo + o) = lo;
       } else {
         for (int i = tid - kBWarps * 32; i < (E0 + E1) * kTcK; i += kExpWarps * 32) {
           const int j = i & (kTcK - 1), p = i / kTcK;
@@ -364,9 +363,17 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spread_tc(const float2* __res
         }
       }
       cp_async_wait_group<kTcAhead - 1>();  // this thread's loads of batch gb + 1 have landed
-      tc::named_sync(1, kBuildThreads);     // (1) done; w0 / w1 and batch gb + 1's records visible
-      // (2) A: builder w takes row groups 2 w, 2 w + 1, then 2 (w + kTcBuilders), ...,
-      // up to the last group holding a row of the tile
+      tc::named_sync(1, kBuildThreads);     // (1) done; stage st free, w0 / w1 and batch gb + 1's records visible
+      // (2) B from registers; A: builder w takes row groups 2 w, 2 w + 1, then
+      // 2 (w + kTcBuilders), ..., up to the last group holding a row of the tile
+      if (warp < kBWarps) {
+        const int q4 = lane >> 3;
+        uint2 hi, lo;
+        tc_split4_f16(vv, hi, lo);
+        const uint32_t o = tc_elem_off(warp, ri, q4 >> 1) + (uint32_t)(q4 & 1) * 8u;
+        *reinterpret_cast<uint2*>(b_hi + o) = hi;
+        *reinterpret_cast<uint2*>(b_lo + o) = lo;
+      }
 #pragma unroll
       for (int i = 0; i < kAIters; ++i) {
         const int rg = 2 * (warp + kTcBuilders * i) + rh;
