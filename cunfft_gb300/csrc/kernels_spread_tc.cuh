@@ -212,8 +212,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spread_tc(const float2* __res
   constexpr int kBuildThreads = kTcBuilders * 32;
   constexpr int kBWarps = kTcN / 8;                             // builders of B: one 8-row group each
   constexpr int kExpWarps = kTcBuilders - kBWarps;              // builders expanding w0 / w1
-  constexpr int kMaxMt = (kTcMaxT0 + W - 1) * E1 / 128 + 1;     // M-tiles at the largest E0
-  constexpr int kAIters = (kMaxMt * 8 + kTcBuilders - 1) / kTcBuilders;  // pairs of row groups per warp
+  // A tasks: (node group kg, row p1) pairs times planes p0; builder thread t takes pair
+  // t % kAPairs and planes t / kAPairs + kAStride i, so its w1 values load once per batch
+  constexpr int kAPairs = 2 * E1;
+  constexpr int kAStride = kBuildThreads / kAPairs;
+  constexpr int kAMaxP = (kTcMaxT0 + W - 1 + kAStride - 1) / kAStride;  // planes per thread at the largest E0
+  static_assert(kAStride >= 1, "every (node group, row) pair needs a builder thread");
   static_assert(2 * E2 <= kTcN, "complex columns must fit the MMA N");
   static_assert(kExpWarps >= 1 && kTcK == 16, "staging roles assume 16 nodes and 8 B-row warps");
   extern __shared__ __align__(16) unsigned char smem[];
@@ -258,24 +262,16 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spread_tc(const float2* __res
   // buffer gb & 1.
   if (warp < kTcBuilders) {
     // ======================= builder warps =======================
-    const int ri = lane & 7, kg = (lane >> 3) & 1, rh = lane >> 4;  // row in group, node group of 8, row group
+    const int ri = lane & 7;  // B build: row in group
     const float* sfrac = reinterpret_cast<const float*>(bins.sfrac);
     const float2* fperm = reinterpret_cast<const float2*>(bins.fperm);
     const float norm = (float)geo.norm;
     const float bscale = norm * tc_scale_b(bins, norm);  // w2 f -> B
-    const int rg_end = (rows + 7) / 8;                   // A row groups holding rows of the tile
+    const int apair = tid % kAPairs, ablk = tid / kAPairs;  // A task: pair and first plane
+    const int akg = apair / E1, ap1 = apair - akg * E1;
+    const bool a_on = ablk < kAStride;
     const float mf = (float)geo.m;
     const TapK k0 = tap_k<WIN>(geo, 0), k1 = tap_k<WIN>(geo, 1), k2 = tap_k<WIN>(geo, 2);
-    // this thread's A rows (row groups 2 (warp + kTcBuilders i) + rh): offsets into wx,
-    // -1 past the tile
-    int a_off0[kAIters], a_off1[kAIters];
-#pragma unroll
-    for (int i = 0; i < kAIters; ++i) {
-      const int r = (2 * (warp + kTcBuilders * i) + rh) * 8 + ri;
-      const int p0 = r / E1, p1 = r - p0 * E1;
-      a_off0[i] = r < rows ? p0 * kTcWxStride + kg * 8 : -1;
-      a_off1[i] = (E0 + p1) * kTcWxStride + kg * 8;
-    }
     // loads of one batch's records into ring slot `slot` (threads < 4 kTcK): thread
     // j < kTcK the window start and sample of node j, thread kTcK + i fraction i
     auto load = [&](const TcCursor& c, int slot) {
@@ -309,11 +305,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spread_tc(const float2* __res
     // A rows past the tile's E0 E1 (up to the M-tiles' 128 L.mt) stay zero: written
     // once here, never by the per-batch builds (published by their proxy fences)
     {
-      const int rg0 = (rows + 7) / 8, ngrp = L.mt * 16 - rg0;
-      for (int i = tid; i < (int)ns * 2 * ngrp * 16; i += kBuildThreads) {
-        const int chunk = i & 15, grp = (i >> 4) % ngrp, part = (i >> 4) / ngrp;  // part: stage x (hi, lo)
+      const int nrow = L.mt * 128 - rows;
+      for (int i = tid; i < (int)ns * 2 * nrow * 2; i += kBuildThreads) {
+        const int g = i & 1, rr = (i >> 1) % nrow, part = (i >> 1) / nrow;  // part: stage x (hi, lo)
+        const int r = rows + rr;
         unsigned char* base = smem + (size_t)(part >> 1) * L.stage_bytes + (size_t)(part & 1) * L.a_bytes;
-        *reinterpret_cast<uint4*>(base + (size_t)(rg0 + grp) * kTcSBO + chunk * 16) = make_uint4(0u, 0u, 0u, 0u);
+        *reinterpret_cast<uint4*>(base + tc_elem_off(r >> 3, r & 7, g)) = make_uint4(0u, 0u, 0u, 0u);
       }
     }
     cp_async_wait_group<kTcAhead - 1>();
@@ -364,8 +361,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spread_tc(const float2* __res
       }
       cp_async_wait_group<kTcAhead - 1>();  // this thread's loads of batch gb + 1 have landed
       tc::named_sync(1, kBuildThreads);     // (1) done; stage st free, w0 / w1 and batch gb + 1's records visible
-      // (2) B from registers; A: builder w takes row groups 2 w, 2 w + 1, then
-      // 2 (w + kTcBuilders), ..., up to the last group holding a row of the tile
+      // (2) B from registers; A: this thread's (node group, row) pair over its planes
       if (warp < kBWarps) {
         const int q4 = lane >> 3;
         uint2 hi, lo;
@@ -374,28 +370,26 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spread_tc(const float2* __res
         *reinterpret_cast<uint2*>(b_hi + o) = hi;
         *reinterpret_cast<uint2*>(b_lo + o) = lo;
       }
+      if (a_on) {
+        const float4 c0 = *reinterpret_cast<const float4*>(wx + (E0 + ap1) * kTcWxStride + akg * 8);
+        const float4 c1 = *reinterpret_cast<const float4*>(wx + (E0 + ap1) * kTcWxStride + akg * 8 + 4);
+        const float cw[8] = {c0.x * kTcScaleA, c0.y * kTcScaleA, c0.z * kTcScaleA, c0.w * kTcScaleA,
+                             c1.x * kTcScaleA, c1.y * kTcScaleA, c1.z * kTcScaleA, c1.w * kTcScaleA};
 #pragma unroll
-      for (int i = 0; i < kAIters; ++i) {
-        const int rg = 2 * (warp + kTcBuilders * i) + rh;
-        if (rg < rg_end) {
-          float v[8];
-#pragma unroll
-          for (int u = 0; u < 8; ++u) v[u] = 0.f;
-          if (a_off0[i] >= 0) {
-            const float4 a0 = *reinterpret_cast<const float4*>(wx + a_off0[i]);
-            const float4 a1 = *reinterpret_cast<const float4*>(wx + a_off0[i] + 4);
-            const float4 c0 = *reinterpret_cast<const float4*>(wx + a_off1[i]);
-            const float4 c1 = *reinterpret_cast<const float4*>(wx + a_off1[i] + 4);
-            v[0] = a0.x * c0.x * kTcScaleA; v[1] = a0.y * c0.y * kTcScaleA;
-            v[2] = a0.z * c0.z * kTcScaleA; v[3] = a0.w * c0.w * kTcScaleA;
-            v[4] = a1.x * c1.x * kTcScaleA; v[5] = a1.y * c1.y * kTcScaleA;
-            v[6] = a1.z * c1.z * kTcScaleA; v[7] = a1.w * c1.w * kTcScaleA;
+        for (int i = 0; i < kAMaxP; ++i) {
+          const int p0 = ablk + kAStride * i;
+          if (p0 < E0) {
+            const float4 a0 = *reinterpret_cast<const float4*>(wx + p0 * kTcWxStride + akg * 8);
+            const float4 a1 = *reinterpret_cast<const float4*>(wx + p0 * kTcWxStride + akg * 8 + 4);
+            const float v[8] = {a0.x * cw[0], a0.y * cw[1], a0.z * cw[2], a0.w * cw[3],
+                                a1.x * cw[4], a1.y * cw[5], a1.z * cw[6], a1.w * cw[7]};
+            uint4 hi, lo;
+            tc_split8_f16(v, hi, lo);
+            const int r = p0 * E1 + ap1;
+            const uint32_t o = tc_elem_off(r >> 3, r & 7, akg);
+            *reinterpret_cast<uint4*>(a_hi + o) = hi;
+            *reinterpret_cast<uint4*>(a_lo + o) = lo;
           }
-          uint4 hi, lo;
-          tc_split8_f16(v, hi, lo);
-          const uint32_t o = tc_elem_off(rg, ri, kg);
-          *reinterpret_cast<uint4*>(a_hi + o) = hi;
-          *reinterpret_cast<uint4*>(a_lo + o) = lo;
         }
       }
       tc::fence_proxy_async_smem();  // generic-proxy operand writes -> tensor core
