@@ -54,11 +54,20 @@ struct TapK {
   float a, b;
 };
 // FP32 tap of the window at distance y (grid units) from the node
+// 2^x by the hardware approximation (ex2.approx.ftz: about 2 ulp, subnormal results
+// flushed to zero); tap exponents lie in [-45, 0], where the flushed range holds
+// weights below 1e-38 that no FP32 sum can see
+__device__ __forceinline__ float tap_exp2(float x) {
+  float r;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
 template <int WIN>
 __device__ __forceinline__ float win_tap(float y, TapK k) {
-  if (WIN == kWinGauss) return exp2f(-(y * y) * k.a);
+  if (WIN == kWinGauss) return tap_exp2(-(y * y) * k.a);
   const float q = (y * y) * k.a, z = 1.f - q;
-  const float e = exp2f(__fdividef(-k.b * q, 1.f + z * rsqrtf(z)));  // NaN for z <= 0, not selected
+  const float e = tap_exp2(__fdividef(-k.b * q, 1.f + z * rsqrtf(z)));  // NaN for z <= 0, not selected
   return z > 0.f ? e : 0.f;
 }
 

@@ -28,7 +28,7 @@
 //    the tile.  Batches are double-buffered (one barrier per batch).  The tile is
 //    then added to the global grid with vector atomics, so neighbouring items'
 //    halos combine.
-//  * Tap weights: exp2f per tap in the FP32 form; in the FP64 form the reference's
+//  * Tap weights: one hardware exp2 per tap in the FP32 form; in the FP64 form the reference's
 //    fast-Gaussian-gridding recurrence (2 exp per node and dim, src/cunfft_kernel.cu:
 //    491-505), which keeps the scarce FP64 pipe on the taps.
 #pragma once
