@@ -391,23 +391,18 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const __grid_consta
     uint32_t gc = 0, gbt = 0;
     float* wt = reinterpret_cast<float*>(smem + L.wt_off) + slot * kItWtStride;  // w0 [0, E0MAX), w1 after
     for (; c0.it < num_items; ++gbt) {
-      // this batch's plane scales (half 0): the loads go out before A of the next batch is built
       const TileOrigin to = decode_tile<3>(geo, tl, c0.item.x);
-      const float* pinv = plane_inv + to.inst * P0 + to.a[0];
-      const int64_t pmax = P0 - to.a[0];  // padded planes left from the tile's first
-      float psc[E0MAX];
-      if (h == 0) {
-#pragma unroll
-        for (int p = 0; p < E0MAX; ++p) psc[p] = p < pmax ? pinv[p] : 0.f;
-      }
+      const float* pinv = plane_inv + to.inst * P0 + to.a[0];  // this tile's plane scales
+      const int pmax = (int)(P0 - to.a[0]);  // padded planes from the tile's first; no window reaches past them
       if (c1.it < num_items) build_a(rn, (gbt + 1u) & 1u);
       const ItRec rnn = it_load_rec(c2, num_items, slot, bins);
       // weight table: half 0 w0 over planes (times each plane's inverse scale and
       // 2^-10), half 1 w1 over rows; the previous batch's readers are past its barrier
       if (h == 0) {
         const int o0 = (int)(rc.off & MASK);
-#pragma unroll
-        for (int p = 0; p < E0MAX; ++p) wt[p] = tc_tap<WIN>(rc.fr0, mf, p - o0, W, k0) * (psc[p] * (1.f / kItScaleA));
+#pragma unroll 4
+        for (int p = 0; p < E0; ++p)
+          wt[p] = p < pmax ? tc_tap<WIN>(rc.fr0, mf, p - o0, W, k0) * (pinv[p] * (1.f / kItScaleA)) : 0.f;
       } else {
         const int o1 = (int)((rc.off >> SH) & MASK);
 #pragma unroll
@@ -458,7 +453,7 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const __grid_consta
 #pragma unroll
         for (int pl = 0; pl < CH; ++pl) {
           const int p0 = c * CH + pl;
-          if (p0 < E0MAX) {
+          if (p0 < E0) {
             const float w0 = wt[p0];
             accx = fmaf(w0, sx[pl], accx);
             accy = fmaf(w0, sy[pl], accy);
