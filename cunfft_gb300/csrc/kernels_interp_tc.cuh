@@ -26,13 +26,14 @@
 // arrays (no wrap), and one thread loads each chunk with four TMA boxes (hi re, hi im,
 // lo re, lo im; 32 halves x E1 rows x CH planes) straight into the 64-byte swizzled
 // K-major layout the MMAs read.  Warp roles: warp 0 lane 0 issues the TMA loads
-// (eight chunk stages), warp 1 lane 0 the MMAs, warps 2-9 (two per lane quarter) build
-// A from their nodes' taps and reduce D.  Hand-offs are mbarriers (the chunk stages'
+// (eight chunk stages), warp 1 lane 0 the MMAs, warps 2-13 (three per lane quarter)
+// prepare their nodes' weights and A and reduce D.  Hand-offs are mbarriers (the chunk stages'
 // with TMA transaction counts); every wait is bounded and a wait that gives up sets
 // the plan's device status flag.
 #pragma once
 
 #include <cuda.h>
+#include <type_traits>
 #include <cuda_fp16.h>
 
 #include "kernels_grid.cuh"
@@ -45,8 +46,9 @@ constexpr int kItK = 32;           // K: innermost tile columns p2 (E2 <= 31), p
 constexpr int kItNodes = 128;      // nodes per batch (MMA M)
 constexpr int kItTmaWarp = 0;
 constexpr int kItMmaWarp = 1;
-constexpr int kItNodeWarp0 = 2;    // 8 node warps: lane quarter = warp % 4, pair half = (warp - 2) / 4
-constexpr int kItNodeWarps = 8;
+constexpr int kItNodeWarp0 = 2;    // 12 node warps: lane quarter = warp % 4, part = (warp - 2) / 4
+constexpr int kItNodeWarps = 12;
+constexpr int kItParts = kItNodeWarps / 4;     // node warps per lane quarter
 constexpr int kItThreads = (2 + kItNodeWarps) * 32;
 constexpr int kItHalf = 64;                    // B rows per part: real parts 0..63, imaginary 64..127
 constexpr int kItN = 2 * kItHalf;              // MMA N
@@ -77,7 +79,7 @@ struct ItLayout {
   uint32_t b_off;      // kItStages chunk stages of kItStage
   uint32_t a_off;      // 2 buffers x (A hi, A lo)
   uint32_t bar_off;    // afull[2], bfull[8], bempty[8], tfull[4], tempty[4]; tensor-memory base
-  uint32_t red_off;    // 2 x 128 float2: the second pair half's partial sums per node
+  uint32_t red_off;    // 2 x 2 x 128 float2: parts 1 and 2's partial sums per node
   uint32_t wt_off;     // [128][kItWtStride] floats: each node's w0 (planes) and w1 (rows) of the batch
   uint32_t total;      // bytes past the aligned base
   uint32_t dyn;        // dynamic shared memory to request (alignment slack included)
@@ -88,9 +90,9 @@ __host__ __device__ constexpr ItLayout it_layout() {
                   kItStages * kItStage,
                   kItStages * kItStage + 4u * kItAPart,
                   kItStages * kItStage + 4u * kItAPart + 256u,
-                  kItStages * kItStage + 4u * kItAPart + 256u + 2048u,
-                  kItStages * kItStage + 4u * kItAPart + 256u + 2048u + 128u * kItWtStride * 4u,
-                  kItStages * kItStage + 4u * kItAPart + 256u + 2048u + 128u * kItWtStride * 4u + 1024u};
+                  kItStages * kItStage + 4u * kItAPart + 256u + 4096u,
+                  kItStages * kItStage + 4u * kItAPart + 256u + 4096u + 128u * kItWtStride * 4u,
+                  kItStages * kItStage + 4u * kItAPart + 256u + 4096u + 128u * kItWtStride * 4u + 1024u};
 }
 
 // Padded split planes of the grid: half [batch][4][P0][P1][P2s], component 0 hi re,
@@ -247,7 +249,7 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const __grid_consta
   const int G = (int)gridDim.x;
 
   if (tid == 0) {
-    for (int i = 0; i < 2; ++i) tc::mbar_init(&afull[i], kItNodeWarps);  // one arrival per node warp
+    for (int i = 0; i < 2; ++i) tc::mbar_init(&afull[i], 4);  // one arrival per A-building (part 2) warp
     for (int i = 0; i < kItStages; ++i) {
       tc::mbar_init(&bfull[i], 1);    // the TMA thread's arrival (+ the boxes' bytes)
       tc::mbar_init(&bempty[i], 1);
@@ -345,13 +347,14 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const __grid_consta
     __syncwarp();
   } else {
     // ======================= node warps: A, then the w0 (x) w1 reduction =======================
-    // Two warps per tensor-memory lane quarter: half h builds A's K values 16 h .. 16 h + 15
-    // of its nodes and reduces the first (h = 0) or second (h = 1) half of each chunk's
-    // (plane, row) pairs; half 1 hands its sums over through shared memory once per batch.
-    // Records are loaded two batches ahead; A of batch gbt + 1 is built at the start
-    // of batch gbt (its buffer's previous batch, gbt - 1, is complete: this thread
-    // waited for all of its accumulators), so the MMAs never wait for A.
-    constexpr int GI0 = (GI + 1) / 2;   // 16-pair groups of half 0
+    // Three warps per tensor-memory lane quarter.  Per batch, part 0 writes its nodes' w0
+    // over the tile's planes (times each plane's inverse scale and 2^-10) and part 1 their
+    // w1 over the rows into a per-node weight table, and part 2 builds A of the next
+    // batch; per chunk, part h reduces the chunk's planes h, h + 3, ...; parts 1 and 2
+    // hand their sums to part 0 through shared memory once per batch.  Records are
+    // loaded two batches ahead; A of batch gbt + 1 is built at the start of batch gbt
+    // (its buffer's previous batch, gbt - 1, is complete: every part waited for all of
+    // its accumulators), so the MMAs never wait for A.
     const int q = warp & 3;             // tensor-memory lane quarter
     const int h = (warp - kItNodeWarp0) >> 2;
     const int slot = 32 * q + lane;     // node slot in the batch = TMEM lane = A row
@@ -365,8 +368,7 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const __grid_consta
       unsigned char* al = ah + kItAPart;
       const int o2 = (int)(r.off >> (2 * SH));
 #pragma unroll
-      for (int kk = 0; kk < kItK / 16; ++kk) {
-        const int k8 = 2 * h + kk;
+      for (int k8 = 0; k8 < kItK / 8; ++k8) {
         float t[8];
 #pragma unroll
         for (int u = 0; u < 8; ++u) t[u] = tc_tap<WIN>(r.fr2, mf, 8 * k8 + u - o2, W, k2) * kItScaleA;
@@ -380,6 +382,45 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const __grid_consta
       tc::fence_proxy_async_smem();
       tc::mbar_arrive_warp(&afull[ab]);
     };
+    // part H's share of one chunk: the accumulator's columns of planes H, H + 3, ...
+    // (16-column groups gmin .. gmax), every load issued before one wait; the columns
+    // are released before the arithmetic
+    auto reduce_part = [&](auto HC, uint32_t t0, uint32_t acc, int c, const float* w1x, const float* wt,
+                           float& ax, float& ay) {
+      constexpr int H = decltype(HC)::value;
+      constexpr int LASTPL = H < CH ? H + ((CH - 1 - H) / 3) * 3 : H;
+      constexpr int GMIN = (H * E1) / 16, GMAX = H < CH ? (LASTPL * E1 + E1 - 1) / 16 : GMIN;
+      constexpr int NG = GMAX - GMIN + 1;
+      float vr[NG][16], vi[NG][16];
+      if (H < CH) {
+#pragma unroll
+        for (int g = 0; g < NG; ++g) {
+          tc::tmem_ld16(t0 + (uint32_t)((GMIN + g) * 16), vr[g]);                    // real parts
+          tc::tmem_ld16(t0 + (uint32_t)kItHalf + (uint32_t)((GMIN + g) * 16), vi[g]);  // imaginary parts
+        }
+        tc::tmem_ld_wait();
+      }
+      tc::fence_before_sync();
+      tc::mbar_arrive_warp(&tempty[acc]);
+      if (H < CH) {
+#pragma unroll
+        for (int pl = H; pl < CH; pl += 3) {
+          float sx = 0.f, sy = 0.f;
+#pragma unroll
+          for (int p1 = 0; p1 < E1; ++p1) {
+            const int col = pl * E1 + p1, g = col / 16 - GMIN, u = col % 16;
+            sx = fmaf(w1x[p1], vr[g][u], sx);
+            sy = fmaf(w1x[p1], vi[g][u], sy);
+          }
+          const int p0 = c * CH + pl;
+          if (p0 < E0) {
+            const float w0 = wt[p0];
+            ax = fmaf(w0, sx, ax);
+            ay = fmaf(w0, sy, ay);
+          }
+        }
+      }
+    };
     ItCursor c0, c1, c2;  // batches gbt, gbt + 1, gbt + 2
     it_cursor_init(c0, bins, num_items);
     c1 = c0;
@@ -387,26 +428,27 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const __grid_consta
     c2 = c1;
     it_cursor_step(c2, bins, num_items);
     ItRec rc = it_load_rec(c0, num_items, slot, bins), rn = it_load_rec(c1, num_items, slot, bins);
-    if (c0.it < num_items) build_a(rc, 0u);
+    if (c0.it < num_items && h == 2) build_a(rc, 0u);
     uint32_t gc = 0, gbt = 0;
     float* wt = reinterpret_cast<float*>(smem + L.wt_off) + slot * kItWtStride;  // w0 [0, E0MAX), w1 after
     for (; c0.it < num_items; ++gbt) {
-      const TileOrigin to = decode_tile<3>(geo, tl, c0.item.x);
-      const float* pinv = plane_inv + to.inst * P0 + to.a[0];  // this tile's plane scales
-      const int pmax = (int)(P0 - to.a[0]);  // padded planes from the tile's first; no window reaches past them
-      if (c1.it < num_items) build_a(rn, (gbt + 1u) & 1u);
       const ItRec rnn = it_load_rec(c2, num_items, slot, bins);
-      // weight table: half 0 w0 over planes (times each plane's inverse scale and
-      // 2^-10), half 1 w1 over rows; the previous batch's readers are past its barrier
+      // weight table (parts 0 and 1) and the next batch's A (part 2); the previous
+      // batch's readers of the table are past its final barrier
       if (h == 0) {
+        const TileOrigin to = decode_tile<3>(geo, tl, c0.item.x);
+        const float* pinv = plane_inv + to.inst * P0 + to.a[0];  // this tile's plane scales
+        const int pmax = (int)(P0 - to.a[0]);  // padded planes from the tile's first; no window reaches past them
         const int o0 = (int)(rc.off & MASK);
 #pragma unroll 4
         for (int p = 0; p < E0; ++p)
           wt[p] = p < pmax ? tc_tap<WIN>(rc.fr0, mf, p - o0, W, k0) * (pinv[p] * (1.f / kItScaleA)) : 0.f;
-      } else {
+      } else if (h == 1) {
         const int o1 = (int)((rc.off >> SH) & MASK);
 #pragma unroll
         for (int p = 0; p < E1; ++p) wt[E0MAX + p] = tc_tap<WIN>(rc.fr1, mf, p - o1, W, k1);
+      } else if (c1.it < num_items) {
+        build_a(rn, (gbt + 1u) & 1u);
       }
       tc::named_sync(1, kItNodeWarps * 32);
       float w1x[E1];
@@ -419,56 +461,19 @@ __global__ void __launch_bounds__(kItThreads, 1) k_interp_tc(const __grid_consta
         healthy &= tc::mbar_wait_warp(&tfull[acc], (gc / kItAcc) & 1u, kItPolls);
         tc::fence_after_sync();
         const uint32_t t0 = tmem + ((uint32_t)(32 * q) << 16) + acc * (uint32_t)kItN;
-        // per plane of the chunk: sum over its rows of w1 times the column, then w0 once
-        float sx[CH], sy[CH];
-#pragma unroll
-        for (int pl = 0; pl < CH; ++pl) sx[pl] = sy[pl] = 0.f;
-        // this half's pair groups (warp-uniform): every load issued, then one wait
-        float vr[GI0][16], vi[GI0][16];
-#pragma unroll
-        for (int gq = 0; gq < GI0; ++gq) {
-          const int gi = h * GI0 + gq;
-          if (gi < GI) {
-            tc::tmem_ld16(t0 + (uint32_t)(gi * 16), vr[gq]);                    // real parts of pairs 16 gi ..
-            tc::tmem_ld16(t0 + (uint32_t)kItHalf + (uint32_t)(gi * 16), vi[gq]);  // imaginary parts
-          }
-        }
-        tc::tmem_ld_wait();
-        tc::fence_before_sync();
-        tc::mbar_arrive_warp(&tempty[acc]);
-#pragma unroll
-        for (int gi = 0; gi < GI; ++gi) {
-          if ((gi >= GI0 ? 1 : 0) != h) continue;
-          const int gq = gi - (gi >= GI0 ? GI0 : 0);
-#pragma unroll
-          for (int u = 0; u < 16; ++u) {
-            const int pr = gi * 16 + u;  // (plane pl, row p1) of the chunk
-            if (pr < NP) {
-              const int pl = pr / E1, p1 = pr - (pr / E1) * E1;
-              sx[pl] = fmaf(w1x[p1], vr[gq][u], sx[pl]);
-              sy[pl] = fmaf(w1x[p1], vi[gq][u], sy[pl]);
-            }
-          }
-        }
-#pragma unroll
-        for (int pl = 0; pl < CH; ++pl) {
-          const int p0 = c * CH + pl;
-          if (p0 < E0) {
-            const float w0 = wt[p0];
-            accx = fmaf(w0, sx[pl], accx);
-            accy = fmaf(w0, sy[pl], accy);
-          }
-        }
+        if (h == 0) reduce_part(std::integral_constant<int, 0>{}, t0, acc, c, w1x, wt, accx, accy);
+        else if (h == 1) reduce_part(std::integral_constant<int, 1>{}, t0, acc, c, w1x, wt, accx, accy);
+        else reduce_part(std::integral_constant<int, 2>{}, t0, acc, c, w1x, wt, accx, accy);
         ++gc;
       }
-      // half 1's sums to half 0 (buffer gbt & 1: half 0 read the other one before this
-      // batch's barrier), which writes the sample
-      float2* rb = red + (gbt & 1u) * 128u;
-      if (h == 1) rb[slot] = make_float2(accx, accy);
+      // parts 1 and 2's sums to part 0 (buffer gbt & 1: part 0 read the other one before
+      // this batch's table barrier), which writes the sample
+      float2* rb = red + (gbt & 1u) * 256u;
+      if (h > 0) rb[(h - 1) * 128 + slot] = make_float2(accx, accy);
       tc::named_sync(1, kItNodeWarps * 32);
       if (h == 0) {
-        const float2 o = rb[slot];
-        if (rc.idx >= 0) f[rc.idx] = make_float2((accx + o.x) * norm, (accy + o.y) * norm);
+        const float2 o1 = rb[slot], o2 = rb[128 + slot];
+        if (rc.idx >= 0) f[rc.idx] = make_float2((accx + o1.x + o2.x) * norm, (accy + o1.y + o2.y) * norm);
       }
       rc = rn;
       rn = rnn;
