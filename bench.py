@@ -121,6 +121,15 @@ def load_peaks():
         return 6800.0, "fallback"
 
 
+def load_tensor_peak():
+    """Dense bf16 TFLOP/s (measured burst; FP16 runs at the same dense rate)."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return float(json.load(fh)["bf16_tflops"]), "measured bf16_tflops (burst)"
+    except Exception:
+        return 1900.0, "fallback"
+
+
 def load_traffic():
     """dram bytes per launch of the dominant kernels from a committed ncu summary."""
     path = os.path.join(ROOT, "profiles", "traffic.json")
@@ -324,6 +333,18 @@ def run_ours(args):
     # plus one evaluation per tap and dimension; FP32 CUDA-core peak (nominal)
     flops = M * W3 * 5 + M * 3 * (2 * M_CUT + 2)
     fp32_peak_tflops = 152 * 128 * 2 * 2.07e9 / 1e12
+    # the tensor-core formulation's MMA work: per node E0 E1 (plane, row) pairs times
+    # 2 E2 (column, re|im) outputs, 2 flops each, for the three FP16 products
+    Wt = 2 * M_CUT + 2
+    T = p32.tiling()["T"]
+    E0, E1, E2 = T[0] + Wt - 1, T[1] + Wt - 1, T[2] + Wt - 1
+    mma_flops = M * E0 * E1 * 2 * E2 * 2 * 3
+    tpeak, tpeak_kind = load_tensor_peak()
+    tensor_roof = {"useful_mma_flops_per_launch": mma_flops,
+                   "achieved_tflops": round(mma_flops / (dom_ms * 1e-3) / 1e12, 1), "peak_tflops": tpeak,
+                   "peak_source": tpeak_kind, "frac": round(mma_flops / (dom_ms * 1e-3) / 1e12 / tpeak, 4),
+                   "note": "FP16 hi/lo products hi*hi + hi*lo + lo*hi on tcgen05 kind::f16; padding rows and "
+                           "columns of the MMA tiles not counted"}
     roofline = {"bound": "hbm", "kernel": dominant, "achieved": round(achieved, 1), "peak": peak,
                 "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": f"{peak_kind} hbm_gbs",
                 "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes,
@@ -332,6 +353,7 @@ def run_ours(args):
                             "peak_tflops": round(fp32_peak_tflops, 1),
                             "peak_source": "nominal FP32 CUDA-core peak, 152 SMs x 128 lanes x 2 flop x 2.07 GHz",
                             "frac": round(flops / (dom_ms * 1e-3) / 1e12 / fp32_peak_tflops, 4)},
+                "tensor": tensor_roof,
                 "spread_ms": round(spread_ms, 4), "interp_ms": round(interp_ms, 4),
                 "taps_per_s": {"spread": M * W3 / (spread_ms * 1e-3), "interp": M * W3 / (interp_ms * 1e-3)}}
 
