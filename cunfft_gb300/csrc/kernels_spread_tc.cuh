@@ -352,12 +352,16 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spread_tc(const float2* __res
           vv[u] = w2 * bscale * (part ? c.y : c.x);
         }
       } else {
-        for (int i = tid - kBWarps * 32; i < (E0 + E1) * kTcK; i += kExpWarps * 32) {
-          const int j = i & (kTcK - 1), p = i / kTcK;
-          const uint32_t off = roff[j];
-          wx[p * kTcWxStride + j] = p < E0 ? tc_tap<WIN>(frac[j * 3 + 0], mf, p - (int)(off & MASK), W, k0)
-                                           : tc_tap<WIN>(frac[j * 3 + 1], mf, (p - E0) - (int)((off >> SH) & MASK), W, k1);
-        }
+        // lane (node j, dimension dd) of expansion warp xw: one load of the node's record,
+        // then the taps of planes (dd = 0) or rows (dd = 1) xw, xw + kExpWarps, ...
+        const int xw = warp - kBWarps, j = lane & (kTcK - 1), dd = lane >> 4;
+        const uint32_t off = roff[j];
+        const float fr = frac[j * 3 + dd];
+        const int o = dd ? (int)((off >> SH) & MASK) : (int)(off & MASK);
+        const int Ed = dd ? E1 : E0;
+        const TapK kd = dd ? k1 : k0;
+        float* const col = wx + (dd ? E0 : 0) * kTcWxStride + j;
+        for (int p = xw; p < Ed; p += kExpWarps) col[p * kTcWxStride] = tc_tap<WIN>(fr, mf, p - o, W, kd);
       }
       cp_async_wait_group<kTcAhead - 1>();  // this thread's loads of batch gb + 1 have landed
       tc::named_sync(1, kBuildThreads);     // (1) done; stage st free, w0 / w1 and batch gb + 1's records visible
