@@ -50,6 +50,7 @@ constexpr int kTcThreads = (kTcBuilders + 1 + 4) * 32;
 constexpr int kTcWarps = kTcThreads / 32;
 constexpr int kTcN = 64;         // MMA N: 2 E2 <= 62 columns (p2, re/im), padded
 constexpr int kTcWxStride = 20;  // floats per expanded-weight row: 8 consecutive rows hit distinct banks
+constexpr int kTcWbStride = 24;  // floats per B-table row: rows two apart start 16 banks apart
 // Node records stream into a ring of kTcRing slots, kTcAhead batches ahead of use.
 // A slot holds [kTcK] packed window starts (int), [kTcK][3] fractions (float) and
 // [kTcK] samples (float2, in sorted order); unused node slots hold a window start
@@ -76,6 +77,8 @@ struct TcLayout {
   uint32_t rec_off;       // kTcRing record slots of kTcSlotBytes
   uint32_t wx_off;        // 2 x ([E0][kTcWxStride] w0 over planes, [E1][kTcWxStride] w1 over rows)
   uint32_t wx_stage;      // bytes of one expanded-weight buffer
+  uint32_t wb_off;        // 2 x [kTcN][kTcWbStride] B values w2 f (rows (p2, re|im), 16 nodes), FP32
+  uint32_t wb_stage;      // bytes of one B-table buffer
   uint32_t bar_off;       // mbarriers full[3], empty[3], acc_full[2], acc_empty[2]; tensor-memory base
   uint32_t total;
   int nacc;               // accumulator buffers in tensor memory (2 when they fit in 512 columns)
@@ -95,7 +98,9 @@ __host__ __device__ inline TcLayout tc_layout(int W, int E0) {
     L.rec_off = ops;
     L.wx_off = L.rec_off + kTcRing * kTcSlotBytes;
     L.wx_stage = (uint32_t)(E0 + E1) * kTcWxStride * 4u;
-    L.bar_off = (L.wx_off + 2u * L.wx_stage + 15u) & ~15u;
+    L.wb_off = (L.wx_off + 2u * L.wx_stage + 15u) & ~15u;
+    L.wb_stage = (uint32_t)kTcN * kTcWbStride * 4u;
+    L.bar_off = L.wb_off + 2u * L.wb_stage;
     L.total = L.bar_off + 96u;
     if (L.total <= 227u * 1024u) break;
   }
@@ -334,22 +339,27 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spread_tc(const float2* __res
       const float* frac = reinterpret_cast<const float*>(sl + kTcSlotFrac);
       const float2* val = reinterpret_cast<const float2*>(sl + kTcSlotVal);
       float* wx = reinterpret_cast<float*>(smem + L.wx_off + (size_t)(gb & 1u) * L.wx_stage);
+      float* wb = reinterpret_cast<float*>(smem + L.wb_off + (size_t)(gb & 1u) * L.wb_stage);
       unsigned char* stage = smem + (size_t)st * L.stage_bytes;
       unsigned char* a_hi = stage;
       unsigned char* a_lo = stage + L.a_bytes;
       unsigned char* b_hi = stage + 2 * L.a_bytes;
       unsigned char* b_lo = b_hi + kTcN * kTcK * 2;
-      // (1) warps 0..7: B row group w (lane: row ri, nodes 4 q4 .. 4 q4 + 3) into registers;
-      // the other builders: w0 and w1 over planes and rows
-      float vv[4];
+      // (1) warps 0..7: lane (node j, half h) of warp w writes the B values w2 f of
+      // columns p2 = 2 w + h and 2 w + h + 16 (rows 2 p2 + re|im of the B table; p2 >= E2
+      // gives zero taps); the other builders: w0 and w1 over planes and rows
       if (warp < kBWarps) {
-        const int q4 = lane >> 3, n = warp * 8 + ri, p2 = n >> 1, part = n & 1;
+        const int j = lane & (kTcK - 1), p2a = 2 * warp + (lane >> 4);
+        const int o = (int)(roff[j] >> (2 * SH));
+        const float fr = frac[j * 3 + 2];
+        const float2 c = val[j];
+        float* const col = wb + j;
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const int j = q4 * 4 + u;
-          const float w2 = tc_tap<WIN>(frac[j * 3 + 2], mf, p2 - (int)(roff[j] >> (2 * SH)), W, k2);
-          const float2 c = val[j];
-          vv[u] = w2 * bscale * (part ? c.y : c.x);
+        for (int i = 0; i < 2; ++i) {
+          const int p2 = p2a + 16 * i;
+          const float w2 = tc_tap<WIN>(fr, mf, p2 - o, W, k2) * bscale;
+          col[(2 * p2) * kTcWbStride] = w2 * c.x;
+          col[(2 * p2 + 1) * kTcWbStride] = w2 * c.y;
         }
       } else {
         // lane (node j, dimension dd) of expansion warp xw: one load of the node's record,
@@ -366,8 +376,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spread_tc(const float2* __res
       cp_async_wait_group<kTcAhead - 1>();  // this thread's loads of batch gb + 1 have landed
       tc::named_sync(1, kBuildThreads);     // (1) done; stage st free, w0 / w1 and batch gb + 1's records visible
       // (2) B from registers; A: this thread's (node group, row) pair over its planes
-      if (warp < kBWarps) {
+      if (warp < kBWarps) {  // row 8 w + ri, nodes 4 q4 .. 4 q4 + 3
         const int q4 = lane >> 3;
+        const float4 t = *reinterpret_cast<const float4*>(wb + (warp * 8 + ri) * kTcWbStride + 4 * q4);
+        const float vv[4] = {t.x, t.y, t.z, t.w};
         uint2 hi, lo;
         tc_split4_f16(vv, hi, lo);
         const uint32_t o = tc_elem_off(warp, ri, q4 >> 1) + (uint32_t)(q4 & 1) * 8u;
