@@ -21,6 +21,17 @@ size_t spread_tc_smem_bytes(const Plan& p) {
   return L.total > floor_bytes ? L.total : floor_bytes;
 }
 
+// Samples in sorted order, read contiguously by the kernels' record loads, and their
+// largest component (the B scale).
+cudaError_t spread_tc_permute(const Plan& p, const void* in, cudaStream_t st) {
+  const int64_t M = p.bins.M;
+  const int pblocks = (int)std::min<int64_t>((M + 255) / 256, (int64_t)p.num_sms * 16);
+  cudaError_t e = cudaMemsetAsync(p.bins.fmax, 0, sizeof(uint32_t), st);
+  if (e != cudaSuccess) return e;
+  k_permute_samples<<<pblocks, 256, 0, st>>>((const float2*)in, p.bins.sidx, M, (float2*)p.bins.fperm, p.bins.fmax);
+  return cudaGetLastError();
+}
+
 template <int W>
 static cudaError_t launch_tc(const Plan& p, const void* in, void* out, cudaStream_t st) {
   if (!spread_tc_supported(p)) return cudaErrorInvalidConfiguration;
@@ -33,17 +44,14 @@ static cudaError_t launch_tc(const Plan& p, const void* in, void* out, cudaStrea
   if (e != cudaSuccess) return e;
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
   if ((size_t)per_sm * tc_layout(W, p.tl.E[0]).tmem_cols > 512u) return cudaErrorInvalidConfiguration;
-  // samples in sorted order, read contiguously by the kernel's record loads
-  const int64_t M = p.bins.M;
-  const int pblocks = (int)std::min<int64_t>((M + 255) / 256, (int64_t)p.num_sms * 16);
-  cudaError_t em = cudaMemsetAsync(p.bins.fmax, 0, sizeof(uint32_t), st);
-  if (em != cudaSuccess) return em;
-  k_permute_samples<<<pblocks, 256, 0, st>>>((const float2*)in, p.bins.sidx, M, (float2*)p.bins.fperm, p.bins.fmax);
+  e = spread_tc_permute(p, in, st);
+  if (e != cudaSuccess) return e;
   kern<<<p.num_sms * per_sm, kTcThreads, smem, st>>>((const float2*)in, (float2*)out, p.geo, p.tl, p.bins);
   return cudaGetLastError();
 }
 
 cudaError_t grid_launch_spread_tc(const Plan& p, const void* in, void* out, cudaStream_t st) {
+  if (spread_tm_supported(p)) return grid_launch_spread_tm(p, in, out, st);
   switch (p.geo.W) {
     case 4: return launch_tc<4>(p, in, out, st);
     case 6: return launch_tc<6>(p, in, out, st);

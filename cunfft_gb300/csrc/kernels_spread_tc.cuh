@@ -195,7 +195,7 @@ __device__ __forceinline__ void cp_async_wait_group() { asm volatile("cp.async.w
 // Samples in sorted order (fp[k] = f[sidx[k]]), so that the spreading kernel's
 // per-batch record loads are contiguous, and their largest |Re|, |Im| into *fmax
 // (float bits: the unsigned order of non-negative floats; zeroed before the launch).
-__global__ void k_permute_samples(const float2* __restrict__ f, const int32_t* __restrict__ sidx, int64_t M,
+static __global__ void k_permute_samples(const float2* __restrict__ f, const int32_t* __restrict__ sidx, int64_t M,
                                   float2* __restrict__ fp, uint32_t* __restrict__ fmax) {
   float mx = 0.f;
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < M; k += (int64_t)gridDim.x * blockDim.x) {

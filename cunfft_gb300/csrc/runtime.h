@@ -122,6 +122,11 @@ cudaError_t grid_launch_spread_reg(const Plan& p, const void* f, void* g, cudaSt
 bool spread_tc_supported(const Plan& p);
 size_t spread_tc_smem_bytes(const Plan& p);
 cudaError_t grid_launch_spread_tc(const Plan& p, const void* f, void* g, cudaStream_t st);
+cudaError_t spread_tc_permute(const Plan& p, const void* f, cudaStream_t st);
+// tensor-core spreading with the A operand in tensor memory (grid_spread_tm.cu); the
+// tensor form runs it whenever the tile's planes fit its four M-tiles
+bool spread_tm_supported(const Plan& p);
+cudaError_t grid_launch_spread_tm(const Plan& p, const void* f, void* g, cudaStream_t st);
 // tensor-core interpolation kernel (grid_interp_tc.cu)
 bool interp_tc_supported(const Plan& p);
 cudaError_t grid_launch_interp_tc(const Plan& p, const void* g, void* f, cudaStream_t st);

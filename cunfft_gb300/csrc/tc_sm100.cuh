@@ -119,6 +119,20 @@ __device__ __forceinline__ void tma_load_5d(void* dst, const void* tmap, int c0,
       : "memory");
 }
 
+// Bulk reduction global[0, bytes) += shared[0, bytes) as FP32 adds, performed by the
+// bulk-copy engine and L2.  Both addresses 16-byte aligned, bytes a multiple of 16.
+// Completion is tracked by this thread's bulk groups.
+__device__ __forceinline__ void bulk_reduce_add_f32(void* gdst, uint32_t ssrc, uint32_t bytes) {
+  asm volatile("cp.reduce.async.bulk.global.shared::cta.bulk_group.add.f32 [%0], [%1], %2;\n" ::"l"(gdst), "r"(ssrc),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;\n" ::: "memory"); }
+// this thread's bulk operations have finished reading their shared-memory sources
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;\n" ::: "memory"); }
+// this thread's bulk operations are complete
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;\n" ::: "memory"); }
+
 // Warp-wide hand-offs on an mbarrier whose count is in warps: one arrival or one
 // poller per (converged) warp instead of 32 same-address operations, which the
 // shared-memory pipe would serialise.  __syncwarp orders every lane's earlier
@@ -139,6 +153,18 @@ __device__ __forceinline__ bool mbar_wait_warp(uint64_t* bar, uint32_t parity, u
 // named barrier among `count` threads (a multiple of 32) of the CTA
 __device__ __forceinline__ void named_sync(uint32_t id, uint32_t count) {
   asm volatile("bar.sync %0, %1;\n" ::"r"(id), "r"(count) : "memory");
+}
+
+// named barrier that also returns, to every participating thread, whether any of them
+// passed cond = true (barrier.red.or): a decision all of them take the same way
+__device__ __forceinline__ bool named_sync_or(uint32_t id, uint32_t count, bool cond) {
+  uint32_t r;
+  asm volatile(
+      "{\n .reg .pred p, q;\n setp.ne.u32 p, %3, 0;\n barrier.cta.red.or.pred q, %1, %2, p;\n selp.u32 %0, 1, 0, q;\n}\n"
+      : "=r"(r)
+      : "r"(id), "r"(count), "r"((uint32_t)cond)
+      : "memory");
+  return r != 0;
 }
 
 // ---- proxy and tcgen05 ordering fences ----
@@ -178,6 +204,17 @@ __device__ __forceinline__ void mma_f16(uint32_t tmem_d, uint64_t adesc, uint64_
       "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
       : "memory");
 }
+// ---- MMA with A in tensor memory: D[tmem] (+)= A[tmem] * B[smem]^T ----
+// A (M = 128 rows, K = 16 FP16) occupies lanes 0..127 of 8 columns from tmem_a: row m
+// in lane m, elements 2c and 2c + 1 in the low and high halves of column c.
+__device__ __forceinline__ void mma_f16_ta(uint32_t tmem_d, uint32_t tmem_a, uint64_t bdesc, uint32_t idesc,
+                                           uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "r"(tmem_a), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
 // arrive on the mbarrier once every previously issued tcgen05 op of this thread completes
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
@@ -199,6 +236,15 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory"); }
+
+// ---- registers -> tensor memory: 32 lanes x 8 consecutive 32-bit columns ----
+// Same lane rule as the loads; thread t writes lane (taddr lane) + t.
+__device__ __forceinline__ void tmem_st8(uint32_t taddr, const uint32_t (&r)[8]) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};\n" ::"r"(taddr), "r"(r[0]),
+               "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7])
+               : "memory");
+}
+__device__ __forceinline__ void tmem_st_wait() { asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory"); }
 
 // ---- FP32 -> (hi, lo) split for 3xTF32 products ----
 // hi = tf32(v) rounded to nearest (low 13 mantissa bits zero), lo = v - hi exactly.
