@@ -481,9 +481,9 @@ def run_ours(args):
         "roofline": roofline,
         # binning 4 (count, scan, scatter, items) + forward 2 (roll-off, interpolation)
         # + adjoint 2 (spreading, roll-off) + the sample permutation of the tensor-core
-        # spreading + the grid split of the tensor-core interpolation
+        # spreading + the plane maxima and FP16 split of the tensor-core interpolation
         "gpu_launches": args.steps * (8 + (1 if p32.spread_kernel() == "tensor" else 0)
-                                      + (1 if p32.interp_kernel() == "tensor" else 0)),
+                                      + (2 if p32.interp_kernel() == "tensor" else 0)),
         "clocks": clk,
     }
     if cpu is not None:
