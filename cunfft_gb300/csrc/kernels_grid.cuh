@@ -220,8 +220,9 @@ __device__ __forceinline__ void load_tile(C* tile, const C* __restrict__ gi, con
   cp_async_wait_all();  // this thread's copies landed; the caller's barrier publishes them
 }
 
-// Add the tile into the global grid.  FP32 pairs (even offset on a grid whose last
-// size is even, so 16-byte aligned and never split by the wrap) go as one float4 atomic.
+// Add the tile into the global grid.  FP32 pairs (even offset on a 16-byte aligned grid
+// whose last size is even, so 16-byte aligned and never split by the wrap) go as one
+// float4 atomic.
 template <int D, int W, typename C>
 __device__ __forceinline__ void flush_tile(const C* tile, C* __restrict__ gi, const Geom& geo, const Tiling& tl,
                                            const TileOrigin& o) {
@@ -231,7 +232,8 @@ __device__ __forceinline__ void flush_tile(const C* tile, C* __restrict__ gi, co
   const int rows = tile_rows<D>(tl);
   constexpr bool kF32 = sizeof(C) == 8;
   const int tid = threadIdx.x, nt = blockDim.x;
-  const bool pairs_ok = kF32 && (n_last & 1) == 0 && (tl.T[D - 1] & 1) == 0;  // even tile origin and row length
+  const bool pairs_ok = kF32 && (n_last & 1) == 0 && (tl.T[D - 1] & 1) == 0 &&  // even tile origin and row length
+                       (reinterpret_cast<uintptr_t>(gi) & 15u) == 0;
   const int per_row = pairs_ok ? (E_last + 1) >> 1 : E_last;
   const int total = rows * per_row;
   for (int e = tid; e < total; e += nt) {

@@ -121,15 +121,31 @@ __device__ __forceinline__ void it_split4_f16(float4 v, uint2& hi, uint2& lo) {
   lo = make_uint2(*reinterpret_cast<const uint32_t*>(&l0), *reinterpret_cast<const uint32_t*>(&l1));
 }
 
+// Four consecutive complex values as two float4 (one 16-byte load each when the
+// address is 16-byte aligned, else four 8-byte loads: a caller's grid may be only
+// 8-byte aligned)
+__device__ __forceinline__ void ld_quad(const float2* src, bool al16, float4& a, float4& b) {
+  if (al16) {
+    a = reinterpret_cast<const float4*>(src)[0];
+    b = reinterpret_cast<const float4*>(src)[1];
+  } else {
+    const float2 v0 = src[0], v1 = src[1], v2 = src[2], v3 = src[3];
+    a = make_float4(v0.x, v0.y, v1.x, v1.y);
+    b = make_float4(v2.x, v2.y, v3.x, v3.y);
+  }
+}
+
 // Largest |Re|, |Im| of every grid plane (instance, i0 < n0) into pmax (float bits,
 // zeroed before the launch): blockIdx.y runs over the plane's quads, blockIdx.x over
 // the planes; one atomic per warp.
 __global__ void k_plane_absmax(const float2* __restrict__ g, uint32_t* __restrict__ pmax, Geom geo) {
   const int64_t plane = blockIdx.x, per = geo.n[1] * geo.n[2] / 4;
-  const float4* src = reinterpret_cast<const float4*>(g + plane * geo.n[1] * geo.n[2]);
+  const float2* src = g + plane * geo.n[1] * geo.n[2];
+  const bool al16 = (reinterpret_cast<uintptr_t>(g) & 15u) == 0;  // n1 n2 is a multiple of 8
   float mx = 0.f;
   for (int64_t e = blockIdx.y * (int64_t)blockDim.x + threadIdx.x; e < per; e += (int64_t)gridDim.y * blockDim.x) {
-    const float4 a = src[2 * e], b = src[2 * e + 1];
+    float4 a, b;
+    ld_quad(src + 4 * e, al16, a, b);
     mx = fmaxf(mx, fmaxf(fmaxf(fmaxf(fabsf(a.x), fabsf(a.y)), fmaxf(fabsf(a.z), fabsf(a.w))),
                          fmaxf(fmaxf(fabsf(b.x), fabsf(b.y)), fmaxf(fabsf(b.z), fabsf(b.w)))));
   }
@@ -161,7 +177,8 @@ __global__ void k_split_pad(const float2* __restrict__ g, const uint32_t* __rest
     const float scale = ldexpf(1.f, kItLogB - ex);
     if (r2 == 0) inv_scale[inst * sd.P0 + i0] = ldexpf(1.f, ex - kItLogB);
     const float2* src = g + gp * geo.n[1] * geo.n[2] + wrap_up(i1, geo.n[1]) * geo.n[2] + wrap_up(i2, geo.n[2]);
-    const float4 a = reinterpret_cast<const float4*>(src)[0], b = reinterpret_cast<const float4*>(src)[1];
+    float4 a, b;
+    ld_quad(src, (reinterpret_cast<uintptr_t>(g) & 15u) == 0, a, b);
     __half* o = out + inst * 4 * comp + (i0 * sd.P1 + i1) * sd.P2s + i2;
     uint2 h, l;
     it_split4_f16(make_float4(a.x * scale, a.z * scale, b.x * scale, b.z * scale), h, l);

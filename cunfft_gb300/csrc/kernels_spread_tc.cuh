@@ -473,6 +473,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spread_tc(const float2* __res
     const int E1a = tl.E[1], E2a = tl.E[2];
     const bool one_wrap = n2 >= E2a;
     const float unscale = 1.f / (kTcScaleA * tc_scale_b(bins, (float)geo.norm));  // a power of two: exact
+    // 16-byte pair atomics need an even row length and a 16-byte aligned grid
+    const bool pairs = (n2 & 1) == 0 && (reinterpret_cast<uintptr_t>(g) & 15u) == 0 && (geo.ntot & 1) == 0;
     uint32_t k = 0;
     int4 nxt = (int)blockIdx.x < num_items ? bins.items[blockIdx.x] : make_int4(0, 0, 0, 0);
     for (int it = blockIdx.x; it < num_items; it += G) {
@@ -508,7 +510,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spread_tc(const float2* __res
                 float2* dst = one_wrap ? (p2 >= kw ? roww : rowa) + p2 : gi + rbase + wrap_up(o.a[2] + p2, n2);
                 const float4 w = make_float4(v[4 * u] * unscale, v[4 * u + 1] * unscale, v[4 * u + 2] * unscale,
                                              v[4 * u + 3] * unscale);
-                if (p2 + 1 < E2a && (n2 & 1) == 0) {  // even row length: the pair is 16-byte aligned
+                if (p2 + 1 < E2a && pairs) {  // the pair is 16-byte aligned
                   if (w.x != 0.f || w.y != 0.f || w.z != 0.f || w.w != 0.f)
                     atomicAdd(reinterpret_cast<float4*>(dst), w);
                 } else {

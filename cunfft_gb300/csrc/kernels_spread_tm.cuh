@@ -370,6 +370,8 @@ __global__ void __launch_bounds__(kTmThreads, 1) k_spread_tm(const float2* __res
     const int E1a = tl.E[1], E2a = tl.E[2];
     const bool one_wrap = n2 >= E2a;
     const float unscale = 1.f / (kTcScaleA * tc_scale_b(bins, (float)geo.norm));  // a power of two: exact
+    // 16-byte pair atomics need an even row length and a 16-byte aligned grid
+    const bool pairs = (n2 & 1) == 0 && (reinterpret_cast<uintptr_t>(g) & 15u) == 0 && (geo.ntot & 1) == 0;
     const int eL = 32 * q + lane, ea = eL / E1, ep1 = eL - ea * E1;
     float* const stg = reinterpret_cast<float*>(smem + L.stg_off) + eL * kTmStgStride;  // + 128 mt rows
     uint32_t k = 0;
@@ -436,7 +438,7 @@ __global__ void __launch_bounds__(kTmThreads, 1) k_spread_tm(const float2* __res
           if (p2 < E2a) {
             const float4 w = *reinterpret_cast<const float4*>(srow + 4 * u);  // scaled when staged
             float2* dst = one_wrap ? (p2 >= kw ? roww : rowa) + p2 : gi + rbase + wrap_up(o.a[2] + p2, n2);
-            if (p2 + 1 < E2a && (n2 & 1) == 0) {  // even row length: the pair is 16-byte aligned
+            if (p2 + 1 < E2a && pairs) {  // the pair is 16-byte aligned
               if (w.x != 0.f || w.y != 0.f || w.z != 0.f || w.w != 0.f) atomicAdd(reinterpret_cast<float4*>(dst), w);
             } else {
               if (w.x != 0.f || w.y != 0.f) atomicAdd(dst, make_float2(w.x, w.y));

@@ -211,3 +211,54 @@ def test_autotune_picks_a_kernel_and_stays_correct(dev):
     assert O.rel_l2(O.nfft_adjoint(x, f, N), p.adjoint(torch.from_numpy(f).to(dev)).cpu()) < TOL32
     p.synchronize()
     p.close()
+
+
+@pytest.mark.parametrize("T0", [8, 16])
+def test_tensor_spreading_grid_alignments(dev, T0):
+    """The tensor-memory-operand form (T0 = 8 at m = 6) adds its staged rows to the grid
+    with 16-byte bulk reductions when the grid is 16-byte aligned and falls back to
+    atomics otherwise; T0 = 16 runs the shared-memory-operand form.  A grid that starts
+    8 bytes into its buffer, and a batched grid (instances ntot apart), match the oracle."""
+    from cunfft_gb300.nfft import NFFT
+    rng = np.random.default_rng(300 + T0)
+    N, M = [32, 32, 32], 20000
+    x = rng.uniform(-0.5, 0.5, (M, 3))
+    f = _rand(M, rng)
+    p = NFFT(N, precision="f32", device=dev).set_nodes(torch.from_numpy(x).to(dev))
+    p.set_tiling([T0])
+    assert p.spread_kernel() == "tensor"
+    ref = O.spread(x, f, N, p.n, 6)
+    ft = torch.from_numpy(f).to(dev).to(torch.complex64)
+    ntot = int(np.prod(p.n))
+    buf = torch.zeros(ntot + 1, dtype=torch.complex64, device=dev)
+    g = buf[1:].view(p.n)
+    assert g.data_ptr() % 16 == 8
+    for k in ("tensor", "register", "shared") if T0 <= 8 else ("tensor", "shared"):
+        p.set_spread_kernel(k)
+        g.zero_()
+        p.spread(ft, g)
+        p.synchronize()
+        assert O.rel_l2(ref, g.cpu().numpy()) < TOL32, k
+        assert buf[0].item() == 0
+    p.set_spread_kernel("auto")
+    assert O.rel_l2(ref, p.spread(ft).cpu().numpy()) < TOL32
+    # interpolation from a grid that starts 8 bytes into its buffer
+    gv = _rand(p.n, rng).astype(np.complex64)
+    g.copy_(torch.from_numpy(gv).to(dev))
+    ref_f = O.interp(x, gv.astype(np.complex128), N, p.n, 6)
+    for k in ("tensor", "shared"):
+        p.set_interp_kernel(k)
+        assert O.rel_l2(ref_f, p.interp(g).cpu().numpy()) < TOL32, k
+        p.synchronize()
+    p.set_interp_kernel("auto")
+    p.close()
+    # two instances with different node sets: instance i's grid starts at i ntot
+    xs = [rng.uniform(-0.5, 0.5, (Mi, 3)) for Mi in (7000, 11000)]
+    fs = [_rand(len(xi), rng) for xi in xs]
+    pb = NFFT(N, precision="f32", batch=2, device=dev)
+    pb.set_nodes(torch.from_numpy(np.concatenate(xs)).to(dev), M_inst=[len(xi) for xi in xs])
+    pb.set_tiling([T0])
+    gb = pb.spread(torch.from_numpy(np.concatenate(fs)).to(dev).to(torch.complex64)).cpu().numpy()
+    for i in range(2):
+        assert O.rel_l2(O.spread(xs[i], fs[i], N, pb.n, 6), gb[i]) < TOL32
+    pb.close()
