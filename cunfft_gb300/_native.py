@@ -87,6 +87,7 @@ X_SYMBOLS = [
     "cunfft_x_spread_noalloc", "cunfft_x_set_spread_kernel", "cunfft_x_get_spread_kernel",
     "cunfft_x_set_window", "cunfft_x_get_window",
     "cunfft_x_set_interp_kernel", "cunfft_x_get_interp_kernel", "cunfft_x_forward_host", "cunfft_x_adjoint_host",
+    "cunfft_x_check_wait_timeout",
 ]
 UTIL_SYMBOLS = [
     "showTimes", "getGPUMemProps_ToStdout", "showCPUMemUse", "showCoeff_double", "showCoeff_cuComplex",
@@ -141,6 +142,7 @@ def lib():
         "cunfft_x_adjoint_host": (ctypes.c_int, [vp, vp, vp]),
         "cunfft_x_stage_times": (ctypes.c_int, [vp, dp, dp, dp, dp]),
         "cunfft_x_synchronize": (ctypes.c_int, [vp]),
+        "cunfft_x_check_wait_timeout": (ctypes.c_int, [vp]),
         "cunfft_x_last_message": (ctypes.c_char_p, [vp]),
         "cunfft_x_status_string": (ctypes.c_char_p, [ctypes.c_int]),
         "cunfft_x_grid": (vp, [vp]),

@@ -123,6 +123,8 @@ bool spread_tc_supported(const Plan& p);
 size_t spread_tc_smem_bytes(const Plan& p);
 cudaError_t grid_launch_spread_tc(const Plan& p, const void* f, void* g, cudaStream_t st);
 cudaError_t spread_tc_permute(const Plan& p, const void* f, cudaStream_t st);
+// failure-reporting check (selftest.cu): a bounded wait that gives up sets *status
+cudaError_t launch_wait_gives_up(int32_t* status, cudaStream_t st);
 // tensor-core spreading with the A operand in tensor memory (grid_spread_tm.cu); the
 // tensor form runs it whenever the tile's planes fit its four M-tiles
 bool spread_tm_supported(const Plan& p);

@@ -218,6 +218,14 @@ int cunfft_x_synchronize(cunfft_x_plan* h) {
   return CUNFFT_X_SUCCESS;
 }
 
+int cunfft_x_check_wait_timeout(cunfft_x_plan* h) {
+  if (!h) return CUNFFT_X_INVALID_ARGUMENT;
+  cg::Plan& p = h->p;
+  if (!p.bins.status) return CUNFFT_X_INVALID_ARGUMENT;
+  const cudaError_t e = cg::launch_wait_gives_up(p.bins.status, p.stream);
+  return e == cudaSuccess ? CUNFFT_X_SUCCESS : cg::check_cuda(&p, e, "k_wait_gives_up launch");
+}
+
 const char* cunfft_x_last_message(const cunfft_x_plan* h) { return h ? h->p.last_msg : ""; }
 
 const char* cunfft_x_status_string(int s) {

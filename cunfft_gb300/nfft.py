@@ -264,6 +264,11 @@ class NFFT:
         nat.check(self._lib.cunfft_x_stage_times(self._h, *[ctypes.byref(a) for a in v]), self._h)
         return dict(zip(("bin", "roc", "fft", "conv"), (a.value for a in v)))
 
+    def check_wait_timeout(self):
+        """Run a kernel whose bounded completion wait gives up (about 1 ms): the next
+        synchronize() raises CunfftError with CUNFFT_X_DEVICE_CHECK_FAILED."""
+        nat.check(self._lib.cunfft_x_check_wait_timeout(self._h), self._h)
+
     def synchronize(self):
         nat.check(self._lib.cunfft_x_synchronize(self._h), self._h)
         self._host_refs = []  # host buffers of finished host-buffer transforms

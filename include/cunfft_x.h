@@ -228,6 +228,14 @@ int cunfft_x_adjoint_host(cunfft_x_plan *plan, const void *f_host, void *fhat_ho
  *  failures (CUNFFT_X_DEVICE_CHECK_FAILED, flag cleared on read). */
 int cunfft_x_synchronize(cunfft_x_plan *plan);
 
+/** Failure-reporting check.  Launches on the plan's stream a one-thread kernel that
+ *  waits, with the bounded mbarrier wait of the tensor-core kernels (here about 1 ms),
+ *  on a barrier nothing arrives on; the wait gives up and sets the plan's device
+ *  status flag as such a kernel would.  The next cunfft_x_synchronize returns
+ *  CUNFFT_X_DEVICE_CHECK_FAILED (and clears the flag); the context stays usable.
+ *  Extension (no reference counterpart). */
+int cunfft_x_check_wait_timeout(cunfft_x_plan *plan);
+
 /** Last error message of a plan (empty string when none). */
 const char *cunfft_x_last_message(const cunfft_x_plan *plan);
 
