@@ -21,9 +21,9 @@
 // M-tile, until the epilogue has read that M-tile of the previous item out.
 //
 // Warp roles (20 warps): 15 builders, one MMA issuer (lane 0), 4 epilogue warps.  Per
-// batch the builders (1) evaluate w0 / w1 over the tile's planes and rows (warps 0-7,
-// lane = node and dimension) and the B values w2 f (warps 8-14, lane = node and
-// column) into shared tables, then after a named barrier among themselves (2) write A
+// batch the builders (1) evaluate w0 / w1 over the tile's planes and rows (lane = node
+// and dimension) and the B values w2 f (lane = node and column) into shared tables
+// (warps 8-14), then after a named barrier among themselves (2) write A
 // (warps 0-7: warp w owns lane quarter w % 4 of M-tiles w / 4 and w / 4 + 2) and split
 // B into its shared-memory stage (warps 8-14).  The epilogue copies each M-tile into
 // shared staging rows and releases it before its atomics.  Hand-offs are mbarriers; every wait
@@ -195,30 +195,31 @@ __global__ void __launch_bounds__(kTmThreads, 1) k_spread_tm(const float2* __res
       const float2* val = reinterpret_cast<const float2*>(sl + kTcSlotVal);
       float* wx = reinterpret_cast<float*>(smem + L.wx_off + (size_t)(gb & 1u) * L.wx_stage);
       float* wb = reinterpret_cast<float*>(smem + L.wb_off + (size_t)(gb & 1u) * L.wb_stage);
-      if (warp < kTmAWarps) {
-        // (1) lane (node j, dimension dd): taps of planes (dd = 0) or rows (dd = 1)
-        // warp, warp + 8, ...
-        const int j = lane & (kTcK - 1), dd = lane >> 4;
+      if (warp >= kTmAWarps) {
+        // (1) the B warps evaluate every table of the batch (the A warps' phase (2) is
+        // the long one): lane (node j, dimension dd) of warp kTmAWarps + w the taps of
+        // planes (dd = 0) or rows (dd = 1) w, w + kTmBWarps, ...; lane (node j, half h)
+        // the B values w2 f of columns p2 = 2 w + h + 2 kTmBWarps i < 32 (p2 >= E2 gives
+        // zero taps)
+        const int bw = warp - kTmAWarps, j = lane & (kTcK - 1), hd = lane >> 4;
         const uint32_t off = roff[j];
-        const float fr = frac[j * 3 + dd];
-        const int o = dd ? (int)((off >> SH) & MASK) : (int)(off & MASK);
-        const int Ed = dd ? E1 : E0;
-        const TapK kd = dd ? k1 : k0;
-        float* const col = wx + (dd ? E0 : 0) * kTcWxStride + j;
-        for (int p = warp; p < Ed; p += kTmAWarps) col[p * kTcWxStride] = tc_tap<WIN>(fr, mf, p - o, W, kd);
-      } else {
-        // (1) lane (node j, half h) of warp kTmAWarps + w: B values w2 f of columns
-        // p2 = 2 w + h + 2 kTmBWarps i < 32 (p2 >= E2 gives zero taps)
-        const int j = lane & (kTcK - 1), p2a = 2 * (warp - kTmAWarps) + (lane >> 4);
-        const int o = (int)(roff[j] >> (2 * SH));
-        const float fr = frac[j * 3 + 2];
+        {
+          const float fr = frac[j * 3 + hd];
+          const int o = hd ? (int)((off >> SH) & MASK) : (int)(off & MASK);
+          const int Ed = hd ? E1 : E0;
+          const TapK kd = hd ? k1 : k0;
+          float* const col = wx + (hd ? E0 : 0) * kTcWxStride + j;
+          for (int p = bw; p < Ed; p += kTmBWarps) col[p * kTcWxStride] = tc_tap<WIN>(fr, mf, p - o, W, kd);
+        }
+        const int o2 = (int)(off >> (2 * SH));
+        const float fr2 = frac[j * 3 + 2];
         const float2 c = val[j];
         float* const col = wb + j;
 #pragma unroll
         for (int i = 0; i < (kTcN / 2 + 2 * kTmBWarps - 1) / (2 * kTmBWarps); ++i) {
-          const int p2 = p2a + 2 * kTmBWarps * i;
+          const int p2 = 2 * bw + hd + 2 * kTmBWarps * i;
           if (p2 >= kTcN / 2) break;
-          const float w2 = tc_tap<WIN>(fr, mf, p2 - o, W, k2) * bscale;
+          const float w2 = tc_tap<WIN>(fr2, mf, p2 - o2, W, k2) * bscale;
           col[(2 * p2) * kTcWbStride] = w2 * c.x;
           col[(2 * p2 + 1) * kTcWbStride] = w2 * c.y;
         }
