@@ -37,7 +37,7 @@
 
 namespace cg {
 
-constexpr int kTmBuilders = 15;                 // warps 0-7: weights + A; warps 8-14: B
+constexpr int kTmBuilders = 15;                 // warps 0-7 write A; warps 8-14 the tables and B
 constexpr int kTmAWarps = 8;
 constexpr int kTmBWarps = kTmBuilders - kTmAWarps;  // 20 warps in all: 96 registers per thread
 constexpr int kTmMmaWarp = kTmBuilders;         // lane 0 issues the MMAs
