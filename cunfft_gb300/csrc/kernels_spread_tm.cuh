@@ -1,8 +1,9 @@
 // kernels_spread_tm.cuh -- 3D FP32 spreading on the tensor cores with the A operand in
 // tensor memory (tcgen05.mma reading A from TMEM, B from shared memory).
 //
-// Same product as k_spread_tc (kernels_spread_tc.cuh): per batch of kTcK = 16 nodes of
-// a tile, D += A B^T with
+// The reference's adjoint gridding (kernelConvWithGauss_adjoint_*, src/cunfft_kernel.cu:
+// 608-1197), with the same window-start rule and taps, as the same product as k_spread_tc
+// (kernels_spread_tc.cuh): per batch of kTcK = 16 nodes of a tile, D += A B^T with
 //     A[(p0, p1), j]     = w0_j[p0 - o0_j] w1_j[p1 - o1_j]      (FP16 hi + lo, x 2^10)
 //     B[(p2, re|im), j]  = w2_j[p2 - o2_j] (Re f_j | Im f_j)    (FP16 hi + lo, x 2^(14 - e))
 // and the three products hi*hi + hi*lo + lo*hi accumulated in FP32.  Here the builder
