@@ -192,21 +192,6 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait_group() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
-// Samples in sorted order (fp[k] = f[sidx[k]]), so that the spreading kernel's
-// per-batch record loads are contiguous, and their largest |Re|, |Im| into *fmax
-// (float bits: the unsigned order of non-negative floats; zeroed before the launch).
-static __global__ void k_permute_samples(const float2* __restrict__ f, const int32_t* __restrict__ sidx, int64_t M,
-                                  float2* __restrict__ fp, uint32_t* __restrict__ fmax) {
-  float mx = 0.f;
-  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < M; k += (int64_t)gridDim.x * blockDim.x) {
-    const float2 v = f[sidx[k]];
-    fp[k] = v;
-    mx = fmaxf(mx, fmaxf(fabsf(v.x), fabsf(v.y)));
-  }
-  const uint32_t m = __reduce_max_sync(0xffffffffu, __float_as_uint(mx));
-  if ((threadIdx.x & 31) == 0 && m != 0u) atomicMax(fmax, m);
-}
-
 template <int W, int WIN>
 __global__ void __launch_bounds__(kTcThreads, 1) k_spread_tc(const float2* __restrict__ f, float2* __restrict__ g,
                                                              Geom geo, Tiling tl, Bins bins) {

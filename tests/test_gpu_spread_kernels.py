@@ -1,4 +1,4 @@
-"""The 3D FP32 spreading kernels (tensor-core 3xTF32, register-tile, shared-tile)
+"""The 3D FP32 spreading kernels (tensor-core FP16 hi + lo, register-tile, shared-tile)
 against each other and the oracle; kernel selection through the extension API."""
 import numpy as np
 import pytest
