@@ -141,9 +141,11 @@ def load_traffic():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+    """nvidia-smi clocks and throttle reasons, sampled every 50 ms from before the timed
+    region (start() returns once sampling is live) to after it; the summary is over the
+    samples stamped inside the region (all samples when none fell inside)."""
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -151,41 +153,64 @@ class ClockSampler:
         self.gpu = gpu_index
         self.proc = None
         self.path = None
+        self.t0 = self.t1 = None
 
     def start(self):
         fd, self.path = tempfile.mkstemp(suffix=".csv")
         os.close(fd)
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
+            return
+        deadline = time.time() + 5.0
+        while time.time() < deadline and os.path.getsize(self.path) == 0:
+            time.sleep(0.01)
+
+    def region(self, begin):
+        """Mark the start (begin=True) or the end of the timed region (host clock)."""
+        import datetime
+        now = datetime.datetime.now()
+        if begin:
+            self.t0 = now
+        else:
+            self.t1 = now
 
     def stop(self):
         if self.proc is None:
             return None
-        time.sleep(0.25)
+        time.sleep(0.1)
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
         except Exception:
             self.proc.kill()
+        import datetime
         rows = []
         for line in open(self.path):
             parts = [p.strip() for p in line.split(",")]
-            if len(parts) >= 9:
+            if len(parts) >= 10:
+                try:
+                    parts[0] = datetime.datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f")
+                except ValueError:
+                    parts[0] = None
                 rows.append(parts)
         os.unlink(self.path)
         if not rows:
             return None
-        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        inside = [r for r in rows if r[0] is not None and self.t0 is not None and self.t1 is not None
+                  and self.t0 <= r[0] <= self.t1 + datetime.timedelta(milliseconds=50)]
+        use = inside or rows
+        sm = [float(r[2]) for r in use if r[2].replace(".", "").isdigit()]
+        mx = [float(r[3]) for r in use if r[3].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        reasons = sorted({names[i] for r in use for i in range(4) if r[6 + i].lower() == "active"})
         load = [s for s in sm if mx and s > 0.5 * max(mx)] or sm
         return {"sm_mhz": statistics.median(load) if load else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(rows)}
+                "reasons": reasons, "samples": len(use), "samples_in_region": len(inside),
+                "interval_ms": 50}
 
 
 def rel_l2(ref, got):
@@ -266,11 +291,13 @@ def run_ours(args):
     clocks = ClockSampler(dev.index)
     clocks.start()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks.region(True)
     e0.record(stream)
     for _ in range(args.steps):
         step32()
     e1.record(stream)
     barrier()
+    clocks.region(False)
     ms32 = e0.elapsed_time(e1) / args.steps
     clk = clocks.stop()
     ms32_max = max_over_ranks(ms32)
