@@ -7,9 +7,16 @@
 // filed under the tile that holds its wrapped window start s_t = u_t mod n_t; the
 // tile-local start o_t = s_t mod T_t and the fraction c_t - m (exact in FP64, then
 // rounded to the plan's real type) are what the gridding kernels need.
+#include "bin_coord.h"
 #include "runtime.h"
 
 namespace cg {
+
+// log2 n_t for power-of-two sizes, else -1: those dimensions reduce x by integer
+// arithmetic on its bits (bin_coord.h), the others in FP64
+struct BinLog2 {
+  int k[kMaxDim];
+};
 
 // bits per dimension of the packed tile-local window start (30 / d)
 __host__ __device__ inline int off_bits_host(int d) { return d == 1 ? 30 : (d == 2 ? 15 : 10); }
@@ -29,7 +36,7 @@ __device__ __forceinline__ void reduce_coord(double x, int64_t n, int m, int64_t
   c = __dsub_rn(nx, (double)u);
 }
 
-__global__ void k_bin_count(const double* __restrict__ x, int64_t M, Geom geo, Tiling tl,
+__global__ void k_bin_count(const double* __restrict__ x, int64_t M, Geom geo, Tiling tl, BinLog2 lg,
                             const int32_t* __restrict__ inst_off, int32_t* __restrict__ count,
                             int2* __restrict__ tile_rank) {
   const int d = geo.d;
@@ -37,8 +44,15 @@ __global__ void k_bin_count(const double* __restrict__ x, int64_t M, Geom geo, T
     int inst = geo.batch > 1 ? find_instance(inst_off, geo.batch, j) : 0;
     int64_t tile = 0;
     for (int t = 0; t < d; ++t) {
-      int64_t u; double c;
-      reduce_coord(x[j * d + t], geo.n[t], geo.m, u, c);
+      const double xt = x[j * d + t];
+      int64_t u;
+      CoordPow2 cp;
+      if (lg.k[t] >= 0 && coord_pow2(xt, lg.k[t], geo.m, cp)) {
+        u = cp.u;
+      } else {
+        double c;
+        reduce_coord(xt, geo.n[t], geo.m, u, c);
+      }
       int64_t s = wrap_n(u, geo.n[t]);
       tile = tile * tl.nb[t] + (s >> (__ffs(tl.T[t]) - 1));  // T_t is a power of two
     }
@@ -48,8 +62,11 @@ __global__ void k_bin_count(const double* __restrict__ x, int64_t M, Geom geo, T
   }
 }
 
+// FP32 fractions on power-of-two sizes come from the integer form: the exact c - m
+// rounded once to FP32 (the FP64 form rounds c to FP64 first; the two differ by at most
+// one FP32 ulp plus 2^-49).  FP64 fractions always take the FP64 form.
 template <typename T>
-__global__ void k_bin_scatter(const double* __restrict__ x, int64_t M, Geom geo, Tiling tl,
+__global__ void k_bin_scatter(const double* __restrict__ x, int64_t M, Geom geo, Tiling tl, BinLog2 lg,
                               const int2* __restrict__ tile_rank, const int32_t* __restrict__ tile_off,
                               int32_t* __restrict__ sidx, int32_t* __restrict__ soff, T* __restrict__ sfrac) {
   const int d = geo.d;
@@ -58,12 +75,22 @@ __global__ void k_bin_scatter(const double* __restrict__ x, int64_t M, Geom geo,
     int64_t pos = (int64_t)tile_off[tr.x] + tr.y;
     uint32_t packed = 0;
     for (int t = 0; t < d; ++t) {
-      int64_t u; double c;
-      reduce_coord(x[j * d + t], geo.n[t], geo.m, u, c);
+      const double xt = x[j * d + t];
+      int64_t u;
+      T frac;
+      CoordPow2 cp;
+      if (sizeof(T) == 4 && lg.k[t] >= 0 && coord_pow2(xt, lg.k[t], geo.m, cp)) {
+        u = cp.u;
+        frac = (T)coord_pow2_frac(cp);
+      } else {
+        double c;
+        reduce_coord(xt, geo.n[t], geo.m, u, c);
+        frac = (T)(c - (double)geo.m);
+      }
       int64_t s = wrap_n(u, geo.n[t]);
       uint32_t o = (uint32_t)(s & (tl.T[t] - 1));  // T_t is a power of two
       packed |= o << (off_bits_host(d) * t);
-      sfrac[pos * d + t] = (T)(c - (double)geo.m);
+      sfrac[pos * d + t] = frac;
     }
     sidx[pos] = (int32_t)j;
     soff[pos] = (int32_t)packed;
@@ -153,19 +180,29 @@ static inline int grid_for(int64_t work, int threads, int sms) {
 cudaError_t launch_binning(const Plan& p, const double* x, cudaStream_t st) {
   const Bins& B = p.bins;
   const Tiling& tl = p.tl;
+  BinLog2 lg;
+  for (int t = 0; t < kMaxDim; ++t) {
+    const int64_t n = t < p.geo.d ? p.geo.n[t] : 0;
+    int k = -1;
+    if (n > 0 && (n & (n - 1)) == 0)
+      for (k = 0; (int64_t(1) << k) < n; ++k) {
+      }
+    lg.k[t] = k;
+  }
   cudaError_t e = cudaMemsetAsync(B.count, 0, sizeof(int32_t) * (tl.tiles_total + 1), st);
   if (e != cudaSuccess) return e;
   if (B.M > 0) {
-    k_bin_count<<<grid_for(B.M, 256, p.num_sms), 256, 0, st>>>(x, B.M, p.geo, tl, B.inst_off, B.count, B.tile_rank);
+    k_bin_count<<<grid_for(B.M, 256, p.num_sms), 256, 0, st>>>(x, B.M, p.geo, tl, lg, B.inst_off, B.count,
+                                                                 B.tile_rank);
   }
   k_scan_tiles<<<1, 1024, 0, st>>>(B.count, tl.tiles_total, tl.chunk, B.tile_off, B.item_off, B.num_items);
   if (B.M > 0) {
     if (p.prec == kF64)
       k_bin_scatter<double><<<grid_for(B.M, 256, p.num_sms), 256, 0, st>>>(
-          x, B.M, p.geo, tl, B.tile_rank, B.tile_off, B.sidx, B.soff, (double*)B.sfrac);
+          x, B.M, p.geo, tl, lg, B.tile_rank, B.tile_off, B.sidx, B.soff, (double*)B.sfrac);
     else
       k_bin_scatter<float><<<grid_for(B.M, 256, p.num_sms), 256, 0, st>>>(
-          x, B.M, p.geo, tl, B.tile_rank, B.tile_off, B.sidx, B.soff, (float*)B.sfrac);
+          x, B.M, p.geo, tl, lg, B.tile_rank, B.tile_off, B.sidx, B.soff, (float*)B.sfrac);
     k_make_items<<<grid_for(tl.tiles_total, 256, p.num_sms), 256, 0, st>>>(B.count, B.tile_off, B.item_off,
                                                                             tl.tiles_total, tl.chunk, B.items);
   }
