@@ -1,0 +1,54 @@
+// Host check of the tensor-core kernels' static resource rules for every supported
+// (W, T0): shared memory within the 227 KB a CTA may use, 16-byte aligned regions,
+// tensor-memory columns within 512, and the M-tile / row mappings covering the tile.
+// Prints one line per failure; exit status 0 when none.
+#include <cstdio>
+
+#include "kernels_interp_tc.cuh"
+#include "kernels_spread_tm.cuh"
+
+using namespace cg;
+
+static int fails = 0;
+#define CHECK(c, ...)              \
+  do {                             \
+    if (!(c)) {                    \
+      std::printf(__VA_ARGS__);    \
+      std::printf("\n");           \
+      ++fails;                     \
+    }                              \
+  } while (0)
+
+int main() {
+  const unsigned kMaxSmem = 227u * 1024u;
+  for (int W = 4; W <= 16; W += 2) {
+    for (int T0 = 1; T0 <= 16; T0 *= 2) {
+      const int E0 = T0 + W - 1, E1 = tm_e1(W);
+      if (spread_tc_ok(3, W, T0)) {
+        const TcLayout L = tc_layout(W, E0);
+        CHECK(L.total <= kMaxSmem, "tc W %d T0 %d: shared %u", W, T0, L.total);
+        CHECK(L.mt * 128 >= E0 * E1, "tc W %d T0 %d: M-tiles", W, T0);
+        CHECK(L.nacc * L.mt * kTcN <= 512 && L.tmem_cols <= 512, "tc W %d T0 %d: tmem", W, T0);
+        CHECK(L.bar_off % 16 == 0 && L.wx_off % 16 == 0 && L.wb_off % 16 == 0, "tc W %d T0 %d: align", W, T0);
+      }
+      if (spread_tm_ok(3, W, T0, E0)) {
+        const TmLayout L = tm_layout(W, E0);
+        CHECK(L.total <= kMaxSmem, "tm W %d T0 %d: shared %u", W, T0, L.total);
+        CHECK(L.mt <= kTmMaxMt && L.mt * tm_ap(W) >= E0 && tm_ap(W) * E1 <= 128, "tm W %d T0 %d: rows", W, T0);
+        CHECK(kTmACol0 + kTmStages * kTmAStageCols <= 512 && (unsigned)(L.mt * kTcN) <= kTmACol0,
+              "tm W %d T0 %d: tmem", W, T0);
+        CHECK(L.rec_off % 16 == 0 && L.wx_off % 16 == 0 && L.wb_off % 16 == 0 && L.bar_off % 16 == 0 &&
+                  L.stg_off % 16 == 0,
+              "tm W %d T0 %d: align", W, T0);
+        CHECK(2 * (fixed_t_last(3, W) + W - 1) <= kTcN, "tm W %d T0 %d: columns", W, T0);
+      }
+      if (interp_tc_ok(3, W, T0, 256)) {
+        const ItLayout L = it_layout();
+        CHECK(L.dyn <= kMaxSmem, "interp W %d T0 %d: shared %u", W, T0, L.dyn);
+        CHECK(it_pairs(W) <= kItHalf && it_ch(W) >= 1, "interp W %d T0 %d: chunk", W, T0);
+      }
+    }
+  }
+  std::printf("layout check: %d failures\n", fails);
+  return fails == 0 ? 0 : 1;
+}
