@@ -122,7 +122,9 @@ int cunfft_x_node_gradient(cunfft_x_plan *plan, const void *f_hat, const void *g
 
 /** Gridding stages alone, on a caller-provided oversampled grid g
  *  (batch*n_total complex, plan precision): interpolation g -> f and
- *  spreading f -> g (spreading accumulates into g; clear it first). */
+ *  spreading f -> g (spreading accumulates into g; clear it first).  g needs only
+ *  the alignment of its element type (8 bytes for FP32 complex); 16-byte aligned
+ *  grids take the wider accesses. */
 int cunfft_x_interp(cunfft_x_plan *plan, const void *g, void *f);
 int cunfft_x_spread(cunfft_x_plan *plan, const void *f, void *g);
 
