@@ -22,6 +22,7 @@ itself is GPU code for a Fermi-era toolchain and does not build here).
 """
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -47,6 +48,9 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-configs", action="store_true", help="skip the clustered, batched and autograd legs")
+    ap.add_argument("--sustain-s", type=float, default=1.0,
+                    help="length of the sustained run after the headline steps (seconds)")
     # The plan's default tiling (T0 = 8, tensor-core kernels) is what the autotuner picks
     # on this workload when timed without a profiler; under ncu its per-launch overhead
     # tips the choice, so the default run skips the autotuner and profiles the same kernels.
@@ -270,6 +274,17 @@ def run_ours(args):
                         torch.rand(M, generator=g, device=dev, dtype=torch.float64) * 2 - 1)
     fh32, f32 = fh64.to(torch.complex64), f64.to(torch.complex64)
     stream = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn, steps):
+        """ms per call of fn over `steps` calls, events on the plan stream, synchronised both sides"""
+        barrier()
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        barrier()
+        return e0.elapsed_time(e1) / steps
 
     # ---------------- FP32 form (headline) ----------------
     p32 = NFFT(N3, m=M_CUT, precision="f32", device=dev)
@@ -285,33 +300,32 @@ def run_ours(args):
         p32.forward(fh32, out=out_f)
         p32.adjoint(f32, out=out_fh)
 
-    for _ in range(max(3, args.warmup)):
+    warm = max(3, args.warmup)
+    for _ in range(warm):
         step32()
     barrier()
     clocks = ClockSampler(dev.index)
     clocks.start()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # the headline: exactly --steps steps, bracketed by a barrier and a synchronize
     clocks.region(True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        step32()
-    e1.record(stream)
-    barrier()
+    ms32 = timed(step32, args.steps)
+    # the same step repeated for at least one second (at least --sustain-s), so that the
+    # clock record holds enough samples and the headline is checked against a long run
+    sus_steps = max(args.steps, int(math.ceil(args.sustain_s * 1e3 / max(ms32, 1e-3))))
+    ms32_sus = timed(step32, sus_steps)
     clocks.region(False)
-    ms32 = e0.elapsed_time(e1) / args.steps
     clk = clocks.stop()
     ms32_max = max_over_ranks(ms32)
+    ms32_sus_max = max_over_ranks(ms32_sus)
 
     # binning amortised: forward + adjoint on an already-binned node set
     p32.set_nodes(x)
-    barrier()
-    e0.record(stream)
-    for _ in range(args.steps):
+
+    def fwdadj32():
         p32.forward(fh32, out=out_f)
         p32.adjoint(f32, out=out_fh)
-    e1.record(stream)
-    barrier()
-    ms32_amort = max_over_ranks(e0.elapsed_time(e1) / args.steps)
+
+    ms32_amort = max_over_ranks(timed(fwdadj32, args.steps))
 
     # stage breakdown of one FP32 step (events on the plan stream)
     p32.set_nodes(x)
@@ -320,8 +334,8 @@ def run_ours(args):
     p32.adjoint(f32, out=out_fh)
     st_a = p32.stage_times()
     stages32 = {"bin_ms": st_f["bin"] * 1e3, "fwd_roc_ms": st_f["roc"] * 1e3, "fwd_fft_ms": st_f["fft"] * 1e3,
-                "fwd_interp_ms": st_f["conv"] * 1e3, "adj_spread_ms": st_a["roc"] * 1e3,
-                "adj_fft_ms": st_a["fft"] * 1e3, "adj_roc_ms": st_a["conv"] * 1e3}
+                "fwd_interp_ms": st_f["conv"] * 1e3, "adj_spread_ms": st_a["conv"] * 1e3,
+                "adj_fft_ms": st_a["fft"] * 1e3, "adj_roc_ms": st_a["roc"] * 1e3}
 
     # ---------------- dominant-kernel roofline (spreading and interpolation alone) ----------------
     grid = p32.grid()
@@ -361,17 +375,23 @@ def run_ours(args):
     flops = M * W3 * 5 + M * 3 * (2 * M_CUT + 2)
     fp32_peak_tflops = 152 * 128 * 2 * 2.07e9 / 1e12
     # the tensor-core formulation's MMA work: per node E0 E1 (plane, row) pairs times
-    # 2 E2 (column, re|im) outputs, 2 flops each, for the three FP16 products
+    # 2 E2 (column, re|im) outputs, 2 flops each, for the three FP16 products; of it
+    # the useful part is the node's own window, W^3 taps x 2 (re|im) x 2 flops x 3
     Wt = 2 * M_CUT + 2
     T = p32.tiling()["T"]
     E0, E1, E2 = T[0] + Wt - 1, T[1] + Wt - 1, T[2] + Wt - 1
     mma_flops = M * E0 * E1 * 2 * E2 * 2 * 3
+    useful_flops = M * W3 * 2 * 2 * 3
     tpeak, tpeak_kind = load_tensor_peak()
-    tensor_roof = {"useful_mma_flops_per_launch": mma_flops,
-                   "achieved_tflops": round(mma_flops / (dom_ms * 1e-3) / 1e12, 1), "peak_tflops": tpeak,
-                   "peak_source": tpeak_kind, "frac": round(mma_flops / (dom_ms * 1e-3) / 1e12 / tpeak, 4),
-                   "note": "FP16 hi/lo products hi*hi + hi*lo + lo*hi on tcgen05 kind::f16; padding rows and "
-                           "columns of the MMA tiles not counted"}
+    tensor_roof = {"issued_mma_flops_per_launch": mma_flops, "useful_mma_flops_per_launch": useful_flops,
+                   "achieved_tflops_issued": round(mma_flops / (dom_ms * 1e-3) / 1e12, 1),
+                   "achieved_tflops_useful": round(useful_flops / (dom_ms * 1e-3) / 1e12, 1),
+                   "peak_tflops": tpeak, "peak_source": tpeak_kind,
+                   "frac_issued": round(mma_flops / (dom_ms * 1e-3) / 1e12 / tpeak, 4),
+                   "frac_useful": round(useful_flops / (dom_ms * 1e-3) / 1e12 / tpeak, 4),
+                   "note": "FP16 hi/lo products hi*hi + hi*lo + lo*hi on tcgen05 kind::f16. Issued: the padded tile's "
+                           "E0 E1 rows x 2 E2 columns per node (padding rows and columns of the MMA tiles not "
+                           "counted); useful: the node's own W^3 window"}
     roofline = {"bound": "hbm", "kernel": dominant, "achieved": round(achieved, 1), "peak": peak,
                 "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": f"{peak_kind} hbm_gbs",
                 "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes,
@@ -394,17 +414,12 @@ def run_ours(args):
         p64.forward(fh64, out=o64f)
         p64.adjoint(f64, out=o64h)
 
-    step64()
-    barrier()
-    k64 = max(2, min(args.steps, 4))
-    e0.record(stream)
-    for _ in range(k64):
+    for _ in range(3):
         step64()
-    e1.record(stream)
-    barrier()
-    ms64 = max_over_ranks(e0.elapsed_time(e1) / k64)
+    k64 = max(20, args.steps)
+    ms64 = max_over_ranks(timed(step64, k64))
 
-    # ---------------- accuracy against the FP64 NDFT ----------------
+    # ---------------- accuracy against the FP64 NDFT, and of the FP32 kernels against the FP64 form ----------------
     gsub = torch.Generator(device=dev).manual_seed(7)
     idx = torch.randperm(M, generator=gsub, device=dev)[:4096]
     kidx = torch.randperm(n_total // 8, generator=gsub, device=dev)[:4096]
@@ -413,36 +428,32 @@ def run_ours(args):
     nd_h = p64.ndft_adjoint_at(f64, kidx)
     p32.set_nodes(x)
     r32f = p32.forward(fh32)
-    r32h = p32.adjoint(f32).reshape(-1)[kidx]
+    r32h_full = p32.adjoint(f32)
+    r32h = r32h_full.reshape(-1)[kidx]
     r64f = o64f[idx]
     r64h = o64h.reshape(-1)[kidx]
     err = {"fp32_forward": rel_l2(nd_f, r32f[idx]), "fp32_adjoint": rel_l2(nd_h, r32h),
            "fp64_forward": rel_l2(nd_f, r64f), "fp64_adjoint": rel_l2(nd_h, r64h)}
+    # the FP32 form against the FP64 form on the same nodes, window and inputs (all 2^21
+    # samples, all 128^3 coefficients): the FP32 kernels' own error, which the window
+    # error against the NDFT (about 1e-6 at m = 6) would hide
+    err_form = {"forward": rel_l2(o64f, r32f), "adjoint": rel_l2(o64h, r32h_full)}
     sub.close()
 
     # ---------------- ES window (cunfft_x_set_window): same step, same NDFT subsamples ----------------
     p64.set_window("es")
     p32.set_window("es")
     step64()
-    barrier()
-    e0.record(stream)
-    for _ in range(k64):
-        step64()
-    e1.record(stream)
-    barrier()
-    ms64_es = max_over_ranks(e0.elapsed_time(e1) / k64)
+    ms64_es = max_over_ranks(timed(step64, k64))
     step32()
-    barrier()
-    e0.record(stream)
-    for _ in range(args.steps):
-        step32()
-    e1.record(stream)
-    barrier()
-    ms32_es = max_over_ranks(e0.elapsed_time(e1) / args.steps)
+    ms32_es = max_over_ranks(timed(step32, args.steps))
+    es_r32f = p32.forward(fh32)
+    es_r32h = p32.adjoint(f32)
     es = {"window": "exponential of semicircle, alpha = m + 1/2, beta = 0.97 pi (2m+1)(1 - 1/(2 sigma))",
-          "fp32": {"value": replica_points_per_s(M, world, ms32_es), "ms_per_step": ms32_es,
-                   "rel_l2_vs_ndft": {"forward": rel_l2(nd_f, p32.forward(fh32)[idx]),
-                                      "adjoint": rel_l2(nd_h, p32.adjoint(f32).reshape(-1)[kidx])}},
+          "fp32": {"value": replica_points_per_s(M, world, ms32_es), "ms_per_step": ms32_es, "steps": args.steps,
+                   "rel_l2_vs_ndft": {"forward": rel_l2(nd_f, es_r32f[idx]),
+                                      "adjoint": rel_l2(nd_h, es_r32h.reshape(-1)[kidx])},
+                   "rel_l2_vs_fp64_form": {"forward": rel_l2(o64f, es_r32f), "adjoint": rel_l2(o64h, es_r32h)}},
           "fp64": {"value": replica_points_per_s(M, world, ms64_es), "ms_per_step": ms64_es, "steps": k64,
                    "rel_l2_vs_ndft": {"forward": rel_l2(nd_f, o64f[idx]), "adjoint": rel_l2(nd_h, o64h.reshape(-1)[kidx])}},
           "ratio_fp32_vs_fp64": ms64_es / ms32_es}
@@ -464,7 +475,7 @@ def run_ours(args):
         p32.forward_host(fhh, fout_h, x=xh)
         p32.adjoint_host(fin_h, fh_h_out)
 
-    for _ in range(max(3, args.warmup)):
+    for _ in range(warm):
         step_e2e()
     p32.synchronize()
     barrier()
@@ -473,32 +484,52 @@ def run_ours(args):
         step_e2e()
     p32.synchronize()
     ms_e2e = max_over_ranks((time.perf_counter() - t0) * 1e3 / args.steps)
-    e2e_err = {"forward": rel_l2(r32f.cpu(), fout_h), "adjoint": rel_l2(p32.adjoint(f32).cpu().reshape(-1),
+    e2e_err = {"forward": rel_l2(r32f.cpu(), fout_h), "adjoint": rel_l2(r32h_full.cpu().reshape(-1),
                                                                        fh_h_out.reshape(-1))}
     h2d = xh.numel() * 8 + fhh.numel() * 8 + fin_h.numel() * 8
     d2h = fout_h.numel() * 8 + fh_h_out.numel() * 8
+    launches_per_step = (4 + 2 + 2 + (1 if p32.spread_kernel() == "tensor" else 0)
+                         + interp_prep_launches(p32))
+    tiling = p32.tiling()
+    p32.close()
+    p64.close()
 
-    # ---------------- CPU baseline (rank 0, N = 1): FP64 direct NDFT on the host ----------------
-    cpu = None
+    # ---------------- the other workloads, each a parity-checked leg of its own ----------------
+    legs = {}
+    if not args.no_configs:
+        legs["clustered_2d"] = leg_clustered_2d(dev, args.steps, timed)
+        legs["batched_2d"] = leg_batched_2d(dev, args.steps, timed)
+        legs["autograd_2d"] = leg_autograd_2d(dev, args.steps, timed)
+
+    # ---------------- CPU baselines (rank 0, N = 1): the reference method and the direct NDFT ----------------
+    cpu = cpu_ndft = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_ndft_baseline(x, fh64, f64)
+        cpu = cpu_reference_method(x, fh64, f64, steps=2)
+        cpu_ndft = cpu_ndft_baseline(x, fh64, f64)
 
     result = {
         "metric": METRIC, "value": replica_points_per_s(M, world, ms32_max), "unit": UNIT, "n_gpus": world,
-        "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms32_max,
+        "steps": args.steps, "warmup": warm, "ms_per_step": ms32_max,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "c64 (f32 taps and accumulation; f64 node reduction and roll-off factors)",
+        "dtype": "c64: gridding on tcgen05 kind::f16 with FP16 hi/lo operands, three products "
+                 "(hi*hi + hi*lo + lo*hi) per tap, FP32 accumulate; FP32 FFT; FP64 node reduction and "
+                 "roll-off factors",
         "data": "synthetic (seeded uniform nodes and coefficients, the reference's 3D workload shape)",
         "config": {"workload": "3D NFFT fwd+adj, N=128^3, n=256^3 (sigma=2), Gaussian m=6, M=2^21 uniform nodes",
                    "step": "bin nodes + forward + adjoint", "form": "FP32", "parallelism": f"replicas x{world}",
                    "l2_cache": "working set (grid 134 MB + nodes 50 MB + coefficients/samples 34 MB) exceeds L2",
-                   "tiling": p32.tiling(), "autotuned": tuned is not None},
+                   "tiling": tiling, "autotuned": tuned is not None},
+        "sustained": {"value": replica_points_per_s(M, world, ms32_sus_max), "ms_per_step": ms32_sus_max,
+                      "steps": sus_steps, "seconds": ms32_sus_max * sus_steps * 1e-3,
+                      "note": "the headline step repeated back to back for at least --sustain-s seconds right "
+                              "after the headline steps; the clock record covers both"},
         "binning_amortised": {"value": replica_points_per_s(M, world, ms32_amort), "ms_per_step": ms32_amort,
                               "step": "forward + adjoint on an already-binned node set"},
         "fp64_plain": {"value": replica_points_per_s(M, world, ms64), "ms_per_step": ms64, "steps": k64},
         "ratio_fp32_vs_fp64": ms64 / ms32_max,
         "es_window": es,
         "rel_l2_vs_ndft": err,
+        "rel_l2_fp32_vs_fp64_form": err_form,
         "stages_fp32": stages32,
         "e2e": {"value": replica_points_per_s(M, world, ms_e2e), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": ms_e2e,
@@ -507,21 +538,274 @@ def run_ours(args):
                 "rel_l2_vs_device_path": e2e_err},
         "roofline": roofline,
         # binning 4 (count, scan, scatter, items) + forward 2 (roll-off, interpolation)
-        # + adjoint 2 (spreading, roll-off) + the sample permutation of the tensor-core
-        # spreading + the plane maxima and FP16 split of the tensor-core interpolation
-        "gpu_launches": args.steps * (8 + (1 if p32.spread_kernel() == "tensor" else 0)
-                                      + (2 if p32.interp_kernel() == "tensor" else 0)),
+        # + adjoint 2 (spreading, crop) + the sample permutation of the tensor-core
+        # spreading + the grid split of the tensor-core interpolation
+        "gpu_launches": args.steps * launches_per_step,
         "clocks": clk,
+        "configs": legs,
     }
     if cpu is not None:
         result["cpu_baseline"] = cpu
-    p32.close()
-    p64.close()
+        result["cpu_ndft"] = cpu_ndft
+        result["fp64_vs_cpu_ratio"] = replica_points_per_s(M, world, ms64) / cpu["value"]
+        result["fp32_vs_cpu_ratio"] = replica_points_per_s(M, world, ms32_max) / cpu["value"]
     if rank == 0:
         print(json.dumps(result))
     if world > 1:
         dist.barrier()
         dist.destroy_process_group()
+
+
+def interp_prep_launches(p):
+    """Launches per forward that prepare the tensor-core interpolation's operands (the
+    grid's per-plane maxima and its FP16 hi/lo split)."""
+    return 2 if p.interp_kernel() == "tensor" else 0
+
+
+def _crand_t(shape, rng, dev, dtype):
+    import torch
+    a = rng.uniform(-1, 1, shape) + 1j * rng.uniform(-1, 1, shape)
+    return torch.from_numpy(a).to(dev, dtype)
+
+
+def clustered_nodes(rng):
+    """512 radial spokes x 1024 samples (uniform angles in [0, pi), radius in [-0.5, 0.5))
+    plus 2^18 nodes from an isotropic Gaussian (std 0.02) at the origin, wrapped to the torus."""
+    import numpy as np
+    spokes, samples = 512, 1024
+    theta = np.pi * np.arange(spokes) / spokes
+    r = -0.5 + np.arange(samples) / samples
+    rad = np.stack([np.outer(np.cos(theta), r).ravel(), np.outer(np.sin(theta), r).ravel()], axis=1)
+    gs = rng.normal(0.0, 0.02, (1 << 18, 2))
+    gs = np.mod(gs + 0.5, 1.0) - 0.5
+    return np.concatenate([rad, gs])
+
+
+def leg_clustered_2d(dev, steps, timed):
+    """2D clustered nodes, N = 512^2, n = 1024^2, m = 6, M = 786,432: FP32 and FP64 forms, a
+    step being bind + forward + adjoint; errors against the FP64 NDFT on 2048 nodes and
+    2048 coefficients, and of the FP32 form against the FP64 form."""
+    import numpy as np
+    import torch
+
+    from cunfft_gb300.nfft import NFFT
+
+    rng = np.random.default_rng(303)
+    N = [512, 512]
+    x = torch.from_numpy(clustered_nodes(rng)).to(dev)
+    M = x.shape[0]
+    fh64 = _crand_t(N, rng, dev, torch.complex128)
+    f64 = _crand_t(M, rng, dev, torch.complex128)
+    fh32, f32 = fh64.to(torch.complex64), f64.to(torch.complex64)
+    out = {}
+    res = {}
+    for prec, fh, f in (("f32", fh32, f32), ("f64", fh64, f64)):
+        p = NFFT(N, m=6, precision=prec, device=dev)
+        of = torch.empty(M, dtype=fh.dtype, device=dev)
+        oh = torch.empty(N, dtype=fh.dtype, device=dev)
+
+        def step():
+            p.set_nodes(x)
+            p.forward(fh, out=of)
+            p.adjoint(f, out=oh)
+
+        for _ in range(3):
+            step()
+        ms = timed(step, steps)
+        p.set_nodes(x)
+        p.forward(fh, out=of)
+        sf = p.stage_times()
+        p.adjoint(f, out=oh)
+        sa = p.stage_times()
+        res[prec] = (of.clone(), oh.clone())
+        out[prec] = {"value": M / (ms * 1e-3), "ms_per_step": ms, "steps": steps,
+                     "stages_ms": {"bin": sf["bin"] * 1e3, "fwd_roc": sf["roc"] * 1e3, "fwd_fft": sf["fft"] * 1e3,
+                                   "fwd_interp": sf["conv"] * 1e3, "adj_spread": sa["conv"] * 1e3,
+                                   "adj_fft": sa["fft"] * 1e3, "adj_roc": sa["roc"] * 1e3},
+                     "kernels": {"spread": p.spread_kernel(), "interp": p.interp_kernel()}}
+        if prec == "f64":
+            gsub = np.random.default_rng(3031)
+            idx = torch.from_numpy(gsub.choice(M, 2048, replace=False)).to(dev)
+            kidx = torch.from_numpy(gsub.choice(N[0] * N[1], 2048, replace=False)).to(dev)
+            sub = NFFT(N, m=6, device=dev).set_nodes(x[idx].contiguous())
+            nd_f = sub.ndft_forward(fh64)
+            nd_h = p.ndft_adjoint_at(f64, kidx)
+            sub.close()
+        p.close()
+    for prec in ("f32", "f64"):
+        of, oh = res[prec]
+        out[prec]["rel_l2_vs_ndft"] = {"forward": rel_l2(nd_f, of[idx]), "adjoint": rel_l2(nd_h, oh.reshape(-1)[kidx])}
+    out["f32"]["rel_l2_vs_fp64_form"] = {"forward": rel_l2(res["f64"][0], res["f32"][0]),
+                                         "adjoint": rel_l2(res["f64"][1], res["f32"][1])}
+    out["workload"] = ("2D NFFT fwd+adj, N=512^2, n=1024^2, Gaussian m=6, M=786432: 512 radial spokes x 1024 "
+                       "samples + 2^18 Gaussian (std 0.02) nodes at the origin")
+    out["M"] = M
+    out["ratio_fp32_vs_fp64"] = out["f64"]["ms_per_step"] / out["f32"]["ms_per_step"]
+    return out
+
+
+def leg_batched_2d(dev, steps, timed):
+    """64 independent 2D instances, N = 256^2, n = 512^2, m = 5, per-instance M log-uniform in
+    [1e3, 1e6], FP32: adjoint + forward replayed from captured CUDA graphs on a bound node set;
+    errors against the FP64 NDFT on 2048 nodes / 2048 coefficients per instance, and of the
+    FP32 form against the FP64 batched form."""
+    import numpy as np
+    import torch
+
+    from cunfft_gb300.nfft import NFFT
+
+    rng = np.random.default_rng(404)
+    B, N, m = 64, [256, 256], 5
+    Ms = np.round(10 ** rng.uniform(3, 6, B)).astype(np.int64)
+    Mt = int(Ms.sum())
+    x = torch.from_numpy(rng.uniform(-0.5, 0.5, (Mt, 2))).to(dev)
+    fh64 = _crand_t([B] + N, rng, dev, torch.complex128)
+    f64 = _crand_t(Mt, rng, dev, torch.complex128)
+    fh32, f32 = fh64.to(torch.complex64), f64.to(torch.complex64)
+    side = torch.cuda.Stream(dev)  # graph capture needs a non-default stream
+    side.wait_stream(torch.cuda.current_stream(dev))
+    with torch.cuda.stream(side):
+        p = NFFT(N, m=m, precision="f32", batch=B, device=dev).set_nodes(x, Ms.tolist())
+        of = torch.empty(Mt, dtype=torch.complex64, device=dev)
+        oh = torch.empty([B] + N, dtype=torch.complex64, device=dev)
+
+        def step():
+            p.adjoint_graph(f32, oh)
+            p.forward_graph(fh32, of)
+
+        for _ in range(3):
+            step()  # the first call of each captures, the others replay
+        side.synchronize()
+    # time on the side stream (where the plan runs)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(side)
+    with torch.cuda.stream(side):
+        for _ in range(steps):
+            step()
+    ev1.record(side)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / steps
+    with torch.cuda.stream(side):
+        p.set_nodes(x, Ms.tolist())
+        p.forward(fh32, out=of)
+        sf = p.stage_times()
+        p.adjoint(f32, out=oh)
+        sa = p.stage_times()
+        kinds = {"spread": p.spread_kernel(), "interp": p.interp_kernel()}
+        p.close()
+    side.synchronize()
+    # FP64 batched form on the same inputs, and the FP64 NDFT on subsamples
+    p64 = NFFT(N, m=m, batch=B, device=dev).set_nodes(x, Ms.tolist())
+    of64 = p64.forward(fh64)
+    oh64 = p64.adjoint(f64)
+    sub_idx, off = [], 0
+    for k in Ms:
+        sub_idx.append(off + rng.choice(int(k), min(2048, int(k)), replace=False))
+        off += int(k)
+    sidx = torch.from_numpy(np.concatenate(sub_idx)).to(dev)
+    sub = NFFT(N, m=m, batch=B, device=dev).set_nodes(x[sidx].contiguous(), [len(s) for s in sub_idx])
+    nd_f = sub.ndft_forward(fh64)
+    kidx = torch.from_numpy(rng.choice(N[0] * N[1], 2048, replace=False)).to(dev)
+    nd_h = p64.ndft_adjoint_at(f64, kidx).reshape(B, -1)
+    err = {"forward": rel_l2(nd_f, of[sidx]), "adjoint": rel_l2(nd_h, oh.reshape(B, -1)[:, kidx])}
+    err_form = {"forward": rel_l2(of64, of), "adjoint": rel_l2(oh64, oh)}
+    sub.close()
+    p64.close()
+    return {"workload": "64 x 2D NFFT adj+fwd, N=256^2, n=512^2, Gaussian m=5, per-instance M log-uniform in "
+                        "[1e3, 1e6], FP32, graph replay on a bound node set",
+            "M": Mt, "value": Mt / (ms * 1e-3), "ms_per_step": ms, "steps": steps,
+            "step": "cunfft_x_adjoint_graph + cunfft_x_forward_graph (two graph launches)",
+            "bin_ms": sf["bin"] * 1e3,
+            "stages_ms": {"fwd_roc": sf["roc"] * 1e3, "fwd_fft": sf["fft"] * 1e3, "fwd_interp": sf["conv"] * 1e3,
+                          "adj_spread": sa["conv"] * 1e3, "adj_fft": sa["fft"] * 1e3, "adj_roc": sa["roc"] * 1e3},
+            "kernels": kinds, "rel_l2_vs_ndft": err, "rel_l2_vs_fp64_form": err_form}
+
+
+def leg_autograd_2d(dev, steps, timed):
+    """Differentiable 2D NFFT, N = 256^2, m = 6, M = 2^18 FP64 nodes: a step is the forward
+    through NFFTFunction and the backward of ||A(x) f_hat - y||^2 (adjoint for f_hat, the
+    derivative-of-window gridding for x); the gradients checked against the exact adjoint
+    and against the FP64 NDFT gradient on 512 nodes."""
+    import numpy as np
+    import torch
+
+    from cunfft_gb300.autograd import NFFTFunction
+    from cunfft_gb300.nfft import NFFT
+
+    rng = np.random.default_rng(505)
+    N, M, m = [256, 256], 1 << 18, 6
+    x0 = rng.uniform(-0.5, 0.5, (M, 2))
+    fh0 = (rng.standard_normal(N) + 1j * rng.standard_normal(N)) / np.sqrt(2)
+    xpert = np.mod(x0 + rng.normal(0, 1e-3, x0.shape) + 0.5, 1.0) - 0.5
+    fhd = torch.from_numpy(fh0).to(dev)
+    yp = NFFT(N, m=m, device=dev).set_nodes(torch.from_numpy(xpert).to(dev))
+    y = yp.forward(fhd)
+    yp.close()
+    plan = NFFT(N, m=m, device=dev)
+    xd = torch.from_numpy(x0).to(dev)
+    state = {}
+
+    def step():
+        xx = xd.clone().requires_grad_(True)
+        fh = fhd.clone().requires_grad_(True)
+        loss = (NFFTFunction.apply(xx, fh, plan) - y).abs().pow(2).sum()
+        loss.backward()
+        state["gx"], state["gfh"] = xx.grad, fh.grad
+
+    for _ in range(3):
+        step()
+    ms = timed(step, steps)
+    with torch.no_grad():
+        r = plan.set_nodes(xd).forward(fhd) - y
+        g_fh = plan.adjoint(2 * r)
+    err_fh = rel_l2(g_fh, state["gfh"])
+    idx = rng.choice(M, 512, replace=False)
+    sub = NFFT(N, m=m, device=dev).set_nodes(torch.from_numpy(x0[idx]).to(dev))
+    k = [torch.arange(-(n // 2), n - n // 2, device=dev, dtype=torch.float64) for n in N]
+    kk = torch.meshgrid(*k, indexing="ij")
+    ref = np.zeros((512, 2))
+    rj = r[torch.from_numpy(idx).to(dev)]
+    for t in range(2):
+        df = sub.ndft_forward((-2j * np.pi) * kk[t] * fhd)
+        ref[:, t] = (torch.conj(2 * rj) * df).real.cpu().numpy()
+    got = state["gx"].cpu().numpy()[idx]
+    err_x = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
+    sub.close()
+    plan.close()
+    return {"workload": "2D NFFT in torch.autograd, N=256^2, n=512^2, Gaussian m=6, M=2^18 FP64 nodes, loss "
+                        "||A(x) f_hat - y||^2",
+            "M": M, "value": M / (ms * 1e-3), "ms_per_step": ms, "steps": steps,
+            "step": "forward (NFFT) + loss + backward (adjoint NFFT + node gradient)",
+            "rel_l2": {"grad_fhat_vs_adjoint": err_fh, "grad_x_vs_fp64_ndft_gradient": err_x}}
+
+
+def cpu_reference_method(x, fh64, f64, steps=2):
+    """The reference method (the oracle's FP64 restatement of the CUNFFT NFFT, OpenMP on
+    all host cores) at the full benchmark size: roll-off, FFT and interpolation, then
+    spreading, FFT and roll-off, timed over `steps` whole steps."""
+    import oracle as O
+
+    xs = x.cpu().numpy()
+    fh = fh64.cpu().numpy()
+    f = f64.cpu().numpy()
+    cores = O.num_threads()
+    ts = [_reference_step(O, xs, fh, f) for _ in range(steps)]
+    t = statistics.median(ts)
+    return {"value": xs.shape[0] / t, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"the whole workload (M = {xs.shape[0]} nodes, N = 128^3): the reference method restated in "
+                      f"C (oracle, FP64, OpenMP {cores} threads), {steps} full forward + adjoint steps, median "
+                      f"{t:.2f} s"}
+
+
+def _reference_step(O, xs, fh, f):
+    n3 = [256, 256, 256]
+    s = time.perf_counter()
+    G = O.fft(O.roc_forward(fh, N3, n3, M_CUT), -1)
+    O.interp(xs, G, N3, n3, M_CUT)
+    Ga = O.fft(O.spread(xs, f, N3, n3, M_CUT), +1)
+    O.roc_adjoint(Ga, N3, n3, M_CUT)
+    return time.perf_counter() - s
 
 
 def cpu_ndft_baseline(x, fh64, f64, sample=None):
@@ -536,7 +820,7 @@ def cpu_ndft_baseline(x, fh64, f64, sample=None):
     f = f64.cpu().numpy()
     cores = O.num_threads()
     if sample is None:
-        sample = max(64, 16 * cores)
+        sample = max(64, 8 * cores)
     rng = np.random.default_rng(3)
     idx = rng.choice(xs.shape[0], sample, replace=False).astype(np.int64)
     kidx = rng.choice(fh.size, sample, replace=False).astype(np.int64)
@@ -565,49 +849,23 @@ def run_reference(args):
 
     cores = O.num_threads()
     rng = np.random.default_rng(20240)
-    n3 = [256, 256, 256]
     fh = rng.uniform(-1, 1, N3) + 1j * rng.uniform(-1, 1, N3)
-    # the node-independent part at full size: roll-off, FFT (both directions)
-    t0 = time.perf_counter()
-    g = O.roc_forward(fh, N3, n3, M_CUT)
-    G = O.fft(g, -1)
-    t1 = time.perf_counter()
-    Ga = O.fft(G, +1)
-    O.roc_adjoint(Ga, N3, n3, M_CUT)
-    t2 = time.perf_counter()
-    t_grid_fixed = t2 - t0
-    budget = 150.0  # seconds for the whole warmup + steps run
-    per_step = max(0.5, budget / max(1, args.steps + args.warmup))
-    # choose the node sample so that one step fits the per-step budget
-    Ms = 1 << 12
-    xs = rng.uniform(-0.5, 0.5, (Ms, 3))
-    fs = rng.uniform(-1, 1, Ms) + 1j * rng.uniform(-1, 1, Ms)
-    a = time.perf_counter()
-    O.interp(xs, G, N3, n3, M_CUT)
-    O.spread(xs, fs, N3, n3, M_CUT)
-    per_node = (time.perf_counter() - a) / Ms
-    Ms = int(min(M_FULL, max(1 << 12, per_step / max(per_node, 1e-9))))
-    xs = rng.uniform(-0.5, 0.5, (Ms, 3))
-    fs = rng.uniform(-1, 1, Ms) + 1j * rng.uniform(-1, 1, Ms)
-
-    def step():
-        s = time.perf_counter()
-        O.interp(xs, G, N3, n3, M_CUT)
-        O.spread(xs, fs, N3, n3, M_CUT)
-        return time.perf_counter() - s
-
+    xs = rng.uniform(-0.5, 0.5, (M_FULL, 3))
+    fs = rng.uniform(-1, 1, M_FULL) + 1j * rng.uniform(-1, 1, M_FULL)
     for _ in range(args.warmup):
-        step()
-    ts = [step() for _ in range(args.steps)]
-    t_nodes = statistics.median(ts) * M_FULL / Ms
-    t_total = t_grid_fixed + t_nodes
-    value = M_FULL / t_total
-    sample = (f"reference method (FP64 CPU restatement, OpenMP {cores} threads): roll-off + FFT at full size "
-              f"({t_grid_fixed:.2f} s, once), gridding on {Ms} of {M_FULL} nodes per step, node part "
-              f"extrapolated linearly")
+        _reference_step(O, xs, fh, fs)
+    t0 = time.perf_counter()
+    ts = [_reference_step(O, xs, fh, fs) for _ in range(args.steps)]
+    wall = time.perf_counter() - t0
+    t_step = wall / max(1, args.steps)
+    value = M_FULL / t_step
+    sample = (f"the whole workload every step (M = {M_FULL} nodes, N = 128^3, no sampling or extrapolation): the "
+              f"reference method restated in C (oracle, FP64, OpenMP {cores} threads), roll-off + FFT + "
+              f"interpolation and spreading + FFT + roll-off; {args.steps} steps in {wall:.1f} s (median step "
+              f"{statistics.median(ts):.2f} s)")
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_total * 1e3, "higher_is_better": True,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "c128 (f64)",
         "data": "synthetic (seeded uniform nodes and coefficients)",
         "config": {"workload": "3D NFFT fwd+adj, N=128^3, n=256^3 (sigma=2), Gaussian m=6, M=2^21 uniform nodes",
@@ -617,8 +875,29 @@ def run_reference(args):
     }))
 
 
+def spawn_local_ranks(args):
+    """--gpus N without a launcher: run N local ranks of this script under
+    torch.distributed.run (one per GPU); with a launcher, WORLD_SIZE must equal N."""
+    if "WORLD_SIZE" in os.environ:
+        world = int(os.environ["WORLD_SIZE"])
+        if world != args.gpus:
+            print(f"bench.py: --gpus {args.gpus} but WORLD_SIZE={world}", file=sys.stderr)
+            sys.exit(2)
+        return False
+    if args.gpus <= 1 or args.impl == "reference":
+        return False
+    import socket
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={args.gpus}",
+           "--master-addr", "127.0.0.1", f"--master-port={port}", os.path.abspath(__file__)] + sys.argv[1:]
+    sys.exit(subprocess.call(cmd))
+
+
 def main():
     args = parse_args()
+    spawn_local_ranks(args)
     if args.case:
         run_case(args)
     elif args.impl == "reference":

@@ -120,7 +120,7 @@ def lib():
         "cunfft_x_forward_graph": (ctypes.c_int, [vp, vp, vp]),
         "cunfft_x_adjoint_graph": (ctypes.c_int, [vp, vp, vp]),
         "cunfft_x_spread_noalloc": (ctypes.c_int, [ctypes.c_int, i64p, i64p, ctypes.c_int, ctypes.c_int,
-                                                   ctypes.c_int64, vp, vp, vp, vp]),
+                                                   ctypes.c_int64, vp, vp, vp, vp, vp]),
         "cunfft_x_ndft_forward": (ctypes.c_int, [vp, vp, vp]),
         "cunfft_x_ndft_adjoint": (ctypes.c_int, [vp, vp, vp]),
         "cunfft_x_ndft_adjoint_at": (ctypes.c_int, [vp, vp, vp, ctypes.c_int64, vp]),

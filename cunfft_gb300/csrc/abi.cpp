@@ -119,13 +119,13 @@ void fill_fg(cunfft_plan* plan) {
 }
 
 int alloc_device(cunfft_plan* plan, AbiState* s) {
-  if (cuda_call(s, cudaMalloc((void**)&plan->g_gpu, sizeof(gpuComplex) * plan->n_total), "cudaMalloc g")) return s->p.last_status;
+  if (cuda_call(s, cg::plan_malloc((void**)&plan->g_gpu, sizeof(gpuComplex) * plan->n_total), "cudaMalloc g")) return s->p.last_status;
   if (cuda_call(s, cudaMemset(plan->g_gpu, 0, sizeof(gpuComplex) * plan->n_total), "cudaMemset g")) return s->p.last_status;
-  if (cuda_call(s, cudaMalloc((void**)&plan->fhat_gpu, sizeof(gpuComplex) * plan->N_total), "cudaMalloc f_hat")) return s->p.last_status;
+  if (cuda_call(s, cg::plan_malloc((void**)&plan->fhat_gpu, sizeof(gpuComplex) * plan->N_total), "cudaMalloc f_hat")) return s->p.last_status;
   if (cuda_call(s, cudaMemset(plan->fhat_gpu, 0, sizeof(gpuComplex) * plan->N_total), "cudaMemset f_hat")) return s->p.last_status;
-  if (cuda_call(s, cudaMalloc((void**)&plan->x_gpu, sizeof(dTyp) * plan->M_total * plan->d + 8), "cudaMalloc x")) return s->p.last_status;
+  if (cuda_call(s, cg::plan_malloc((void**)&plan->x_gpu, sizeof(dTyp) * plan->M_total * plan->d + 8), "cudaMalloc x")) return s->p.last_status;
   if (cuda_call(s, cudaMemset(plan->x_gpu, 0, sizeof(dTyp) * plan->M_total * plan->d + 8), "cudaMemset x")) return s->p.last_status;
-  if (cuda_call(s, cudaMalloc((void**)&plan->f_gpu, sizeof(gpuComplex) * plan->M_total + 16), "cudaMalloc f")) return s->p.last_status;
+  if (cuda_call(s, cg::plan_malloc((void**)&plan->f_gpu, sizeof(gpuComplex) * plan->M_total + 16), "cudaMalloc f")) return s->p.last_status;
   if (cuda_call(s, cudaMemset(plan->f_gpu, 0, sizeof(gpuComplex) * plan->M_total + 16), "cudaMemset f")) return s->p.last_status;
   return CUNFFT_X_SUCCESS;
 }

@@ -50,9 +50,9 @@ cudaError_t interp_tc_prepare(Plan& p) {
   PFN_cuTensorMapEncodeTiled_v12000 enc = encode_tiled();
   if (!enc) return cudaErrorNotSupported;
   if (!p.it_split) {
-    cudaError_t e = cudaMalloc(&p.it_split, bytes);
-    if (e == cudaSuccess) e = cudaMalloc(&p.it_pinv, sizeof(float) * (size_t)(sd.P0 * p.geo.batch));
-    if (e == cudaSuccess) e = cudaMalloc(&p.it_pmax, sizeof(uint32_t) * (size_t)(p.geo.n[0] * p.geo.batch));
+    cudaError_t e = plan_malloc(&p.it_split, bytes);
+    if (e == cudaSuccess) e = plan_malloc(&p.it_pinv, sizeof(float) * (size_t)(sd.P0 * p.geo.batch));
+    if (e == cudaSuccess) e = plan_malloc(&p.it_pmax, sizeof(uint32_t) * (size_t)(p.geo.n[0] * p.geo.batch));
     if (e != cudaSuccess) {
       interp_tc_release(p);
       return e;

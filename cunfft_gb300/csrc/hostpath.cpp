@@ -48,8 +48,8 @@ static int host_path(Plan* p, HostPath** out) {
                         &h->fh_in,     &h->f_in,      &h->f_out_done, &h->fh_out_done};
   for (cudaEvent_t* e : evs) CG_TRY(check_cuda(p, cudaEventCreateWithFlags(e, cudaEventDisableTiming), "cudaEventCreate"));
   const size_t coef = plan_elem_bytes(p) * (size_t)p->geo.Ntot * (size_t)p->geo.batch;
-  CG_TRY(check_cuda(p, cudaMalloc(&h->fh_in_dev, coef), "cudaMalloc host-path staging"));
-  CG_TRY(check_cuda(p, cudaMalloc(&h->fh_out_dev, coef), "cudaMalloc host-path staging"));
+  CG_TRY(check_cuda(p, plan_malloc(&h->fh_in_dev, coef), "cudaMalloc host-path staging"));
+  CG_TRY(check_cuda(p, plan_malloc(&h->fh_out_dev, coef), "cudaMalloc host-path staging"));
   *out = h;
   return CUNFFT_X_SUCCESS;
 }
@@ -70,9 +70,9 @@ static int host_path_nodes(Plan* p, HostPath* h, int64_t M) {
   h->cap_M = -1;
   const int64_t cap = std::max<int64_t>(M, 1);
   for (int b = 0; b < 2; ++b)
-    CG_TRY(check_cuda(p, cudaMalloc(&h->x[b], sizeof(double) * (size_t)cap * p->geo.d), "cudaMalloc host-path staging"));
-  CG_TRY(check_cuda(p, cudaMalloc(&h->f_in_dev, plan_elem_bytes(p) * (size_t)cap), "cudaMalloc host-path staging"));
-  CG_TRY(check_cuda(p, cudaMalloc(&h->f_out_dev, plan_elem_bytes(p) * (size_t)cap), "cudaMalloc host-path staging"));
+    CG_TRY(check_cuda(p, plan_malloc(&h->x[b], sizeof(double) * (size_t)cap * p->geo.d), "cudaMalloc host-path staging"));
+  CG_TRY(check_cuda(p, plan_malloc(&h->f_in_dev, plan_elem_bytes(p) * (size_t)cap), "cudaMalloc host-path staging"));
+  CG_TRY(check_cuda(p, plan_malloc(&h->f_out_dev, plan_elem_bytes(p) * (size_t)cap), "cudaMalloc host-path staging"));
   h->cap_M = cap;
   return CUNFFT_X_SUCCESS;
 }

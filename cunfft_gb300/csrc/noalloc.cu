@@ -1,20 +1,25 @@
 // noalloc.cu -- spreading entry point that allocates no memory.
 //
-// Some callers cannot call cudaMalloc: code that records work into a CUDA graph
-// through stream capture (allocation is not a capturable operation), frameworks
-// that own all device memory through their own pool allocator, and real-time
-// loops that must not risk an allocation's latency or failure mid-run.  For them
-// cunfft_x_spread_noalloc bins the nodes and spreads them with the same kernels
-// as cunfft_x_spread, but keeps all of its scratch (the sorted node records,
-// per-tile counts and offsets, work items and queue counters) in one fixed
-// file-scope device array instead of plan-owned allocations.
+// Some callers cannot call cudaMalloc: frameworks whose device memory all belongs to
+// their own pool allocator (a side allocation can fail once the pool has reserved the
+// device, or fragment it), real-time loops that must not pay an allocation's latency
+// or risk its failure mid-run, and host applications that forbid allocation inside
+// their plug-in callbacks.  For them cunfft_x_spread_noalloc bins the nodes and
+// spreads them with the same kernels as cunfft_x_spread, but keeps all of its scratch
+// (the sorted node records, per-tile counts and offsets, work items, queue counters
+// and the device status word) in one fixed file-scope device array instead of
+// plan-owned allocations.
 //
-// That array is part of the library's device image: every GPU on which the
-// library is loaded holds it (about 58 MB) until the process exits.  All calls
-// share it, so calls that overlap on the GPU (concurrent streams, or host
-// threads driving the same device) race on it and must be serialised by the
-// caller.  Every call rewrites all scratch it reads: the per-tile counts and the
-// work-queue counters are cleared on the stream before use.
+// That array is part of the library's device image: every GPU on which the library
+// is loaded holds it (about 58 MB) until the process exits.  All calls share it, so
+// calls that overlap on the GPU (concurrent streams, or host threads driving the same
+// device) race on it and must be serialised by the caller.  Every call rewrites all
+// scratch it reads: the per-tile counts, the work-queue counters and the status word
+// are cleared on the stream before use.
+//
+// The array's device address is looked up once per device and cached; a device reset
+// (cudaDeviceReset) unloads the module, after which the cached address is stale, so
+// the entry point must not be used across a device reset.
 #include <mutex>
 #include <stdio.h>
 
@@ -80,7 +85,7 @@ cudaError_t na_scratch(unsigned char** out) {
 }  // namespace cg
 
 extern "C" int cunfft_x_spread_noalloc(int d, const int64_t* N, const int64_t* n, int m, int precision, int64_t M,
-                                       const double* x, const void* f, void* g, void* stream) {
+                                       const double* x, const void* f, void* g, void* stream, int32_t* status) {
   using namespace cg;
   if (!N || M < 0 || (M > 0 && (!x || !f)) || !g) {
     fprintf(stderr, "cunfft_x_spread_noalloc: invalid argument (NULL pointer or M < 0)\n");
@@ -114,6 +119,14 @@ extern "C" int cunfft_x_spread_noalloc(int d, const int64_t* N, const int64_t* n
     fprintf(stderr, "cunfft_x_spread_noalloc: scratch address lookup failed: %s\n", cudaGetErrorString(e));
     return CUNFFT_X_CUDA_ERROR;
   }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  // the kernels' device status word: the caller's, or the scratch copy; cleared per call
+  int32_t* status_word = status ? status : reinterpret_cast<int32_t*>(base + kOffStatus);
+  if ((e = cudaMemsetAsync(status_word, 0, sizeof(int32_t), st)) != cudaSuccess) {
+    fprintf(stderr, "cunfft_x_spread_noalloc: clearing the status word failed: %s\n", cudaGetErrorString(e));
+    return CUNFFT_X_CUDA_ERROR;
+  }
+  if (M == 0) return CUNFFT_X_SUCCESS;  // nothing to spread: g stays as it is
   Bins& B = p.bins;
   B.sidx = reinterpret_cast<int32_t*>(base + kOffSidx);
   B.soff = reinterpret_cast<int32_t*>(base + kOffSoff);
@@ -127,14 +140,13 @@ extern "C" int cunfft_x_spread_noalloc(int d, const int64_t* N, const int64_t* n
   B.num_items = reinterpret_cast<int32_t*>(base + kOffNumItems);
   B.work = reinterpret_cast<int32_t*>(base + kOffWork);
   B.inst_off = reinterpret_cast<int32_t*>(base + kOffInstOff);  // unused for one instance
-  B.status = reinterpret_cast<int32_t*>(base + kOffStatus);
+  B.status = status_word;
   B.fmax = reinterpret_cast<uint32_t*>(base + kOffFmax);
   B.M = M;
   B.max_items = kNaMaxItems;
   B.valid = 1;
   p.M = M;
   p.x = x;
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
   if ((e = launch_binning(p, x, st)) != cudaSuccess || (e = launch_spread(p, f, g, st)) != cudaSuccess) {
     fprintf(stderr, "cunfft_x_spread_noalloc: launch failed: %s\n", cudaGetErrorString(e));
     return CUNFFT_X_CUDA_ERROR;

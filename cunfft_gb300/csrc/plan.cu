@@ -11,6 +11,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <vector>
 
 #include "runtime.h"
@@ -42,6 +43,28 @@ int check_cufft(Plan* p, cufftResult r, const char* what) {
   if (r == CUFFT_SUCCESS) return CUNFFT_X_SUCCESS;
   return set_status(p, r == CUFFT_ALLOC_FAILED ? CUNFFT_X_ALLOC_FAILED : CUNFFT_X_CUFFT_ERROR,
                     "%s: cuFFT error %d", what, (int)r);
+}
+
+// Fault points of the error-path tests: the environment value k (0 or unset: off)
+// selects the k-th call of the process, counted from 1.
+static long fault_point_env(const char* name) {
+  const char* v = getenv(name);
+  return v ? atol(v) : 0;
+}
+static std::atomic<long> g_alloc_calls{0}, g_fft_calls{0};
+
+cudaError_t plan_malloc(void** ptr, size_t bytes) {
+  static const long k = fault_point_env("CUNFFT_X_FAULT_ALLOC");
+  if (k > 0 && g_alloc_calls.fetch_add(1) + 1 == k) {
+    *ptr = nullptr;
+    return cudaErrorMemoryAllocation;
+  }
+  return cudaMalloc(ptr, bytes);
+}
+
+bool plan_fft_fault() {
+  static const long k = fault_point_env("CUNFFT_X_FAULT_CUFFT");
+  return k > 0 && g_fft_calls.fetch_add(1) + 1 == k;
 }
 
 static bool is_pow2(int64_t v) { return v > 0 && (v & (v - 1)) == 0; }
@@ -382,7 +405,7 @@ int plan_init(Plan* p, int d, const int64_t* N, const int64_t* n, int m, int pre
   // roll-off factor tables, per dimension
   {
     const std::vector<double> tab = roc_factors(g);
-    CG_TRY(check_cuda(p, cudaMalloc(&p->roc_tab, sizeof(double) * tab.size()), "cudaMalloc roll-off table"));
+    CG_TRY(check_cuda(p, plan_malloc(&p->roc_tab, sizeof(double) * tab.size()), "cudaMalloc roll-off table"));
     CG_TRY(check_cuda(p, cudaMemcpy(p->roc_tab, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice),
                       "upload roll-off table"));
   }
@@ -390,7 +413,7 @@ int plan_init(Plan* p, int d, const int64_t* N, const int64_t* n, int m, int pre
     p->g = lend_grid;
     p->own_g = false;
   } else {
-    CG_TRY(check_cuda(p, cudaMalloc(&p->g, elem_bytes(p) * g.ntot * batch), "cudaMalloc grid"));
+    CG_TRY(check_cuda(p, plan_malloc(&p->g, elem_bytes(p) * g.ntot * batch), "cudaMalloc grid"));
     p->own_g = true;
   }
   // batched in-place FFT over the instances' grids
@@ -405,8 +428,9 @@ int plan_init(Plan* p, int d, const int64_t* N, const int64_t* n, int m, int pre
     size_t ws = 0;
     long long nll[kMaxDim];
     for (int t = 0; t < d; ++t) nll[t] = nn[t];
-    cufftResult r = cufftMakePlanMany64(h, d, nll, nullptr, 1, g.ntot, nullptr, 1, g.ntot,
-                                        prec == kF64 ? CUFFT_Z2Z : CUFFT_C2C, batch, &ws);
+    cufftResult r = plan_fft_fault() ? CUFFT_INTERNAL_ERROR
+                                     : cufftMakePlanMany64(h, d, nll, nullptr, 1, g.ntot, nullptr, 1, g.ntot,
+                                                           prec == kF64 ? CUFFT_Z2Z : CUFFT_C2C, batch, &ws);
     if (r != CUFFT_SUCCESS) {
       cufftDestroy(h);
       return check_cufft(p, r, "cufftMakePlanMany64");
@@ -415,11 +439,11 @@ int plan_init(Plan* p, int d, const int64_t* N, const int64_t* n, int m, int pre
     p->own_fft = true;
   }
   // per-instance node offsets, status flag, work counters
-  CG_TRY(check_cuda(p, cudaMalloc(&p->bins.inst_off, sizeof(int32_t) * (batch + 1)), "cudaMalloc"));
-  CG_TRY(check_cuda(p, cudaMalloc(&p->bins.work, sizeof(int32_t) * 2), "cudaMalloc"));
-  CG_TRY(check_cuda(p, cudaMalloc(&p->bins.num_items, sizeof(int32_t)), "cudaMalloc"));
-  CG_TRY(check_cuda(p, cudaMalloc(&p->bins.status, sizeof(int32_t)), "cudaMalloc"));
-  CG_TRY(check_cuda(p, cudaMalloc(&p->bins.fmax, sizeof(uint32_t)), "cudaMalloc"));
+  CG_TRY(check_cuda(p, plan_malloc(&p->bins.inst_off, sizeof(int32_t) * (batch + 1)), "cudaMalloc"));
+  CG_TRY(check_cuda(p, plan_malloc(&p->bins.work, sizeof(int32_t) * 2), "cudaMalloc"));
+  CG_TRY(check_cuda(p, plan_malloc(&p->bins.num_items, sizeof(int32_t)), "cudaMalloc"));
+  CG_TRY(check_cuda(p, plan_malloc(&p->bins.status, sizeof(int32_t)), "cudaMalloc"));
+  CG_TRY(check_cuda(p, plan_malloc(&p->bins.fmax, sizeof(uint32_t)), "cudaMalloc"));
   CG_TRY(check_cuda(p, cudaMemset(p->bins.status, 0, sizeof(int32_t)), "cudaMemset"));
   p->M_inst = (int64_t*)calloc((size_t)batch, sizeof(int64_t));
   CG_TRY(plan_choose_tiling(p, nullptr, 0));
@@ -470,16 +494,16 @@ static int ensure_bins(Plan* p, int64_t M) {
       p->bins_capacity_M < 0) {
     const int64_t capM = std::max<int64_t>(M, 1), capT = tiles;
     free_bins(p);
-    CG_TRY(check_cuda(p, cudaMalloc(&B.sidx, sizeof(int32_t) * capM), "cudaMalloc bins"));
-    CG_TRY(check_cuda(p, cudaMalloc(&B.soff, sizeof(int32_t) * capM), "cudaMalloc bins"));
-    CG_TRY(check_cuda(p, cudaMalloc(&B.sfrac, real * p->geo.d * capM), "cudaMalloc bins"));
-    CG_TRY(check_cuda(p, cudaMalloc(&B.tile_rank, sizeof(int2) * capM), "cudaMalloc bins"));
-    CG_TRY(check_cuda(p, cudaMalloc(&B.fperm, elem_bytes(p) * capM), "cudaMalloc bins"));
-    CG_TRY(check_cuda(p, cudaMalloc(&B.count, sizeof(int32_t) * (capT + 1)), "cudaMalloc bins"));
-    CG_TRY(check_cuda(p, cudaMalloc(&B.tile_off, sizeof(int32_t) * (capT + 1)), "cudaMalloc bins"));
-    CG_TRY(check_cuda(p, cudaMalloc(&B.item_off, sizeof(int32_t) * (capT + 1)), "cudaMalloc bins"));
+    CG_TRY(check_cuda(p, plan_malloc(&B.sidx, sizeof(int32_t) * capM), "cudaMalloc bins"));
+    CG_TRY(check_cuda(p, plan_malloc(&B.soff, sizeof(int32_t) * capM), "cudaMalloc bins"));
+    CG_TRY(check_cuda(p, plan_malloc(&B.sfrac, real * p->geo.d * capM), "cudaMalloc bins"));
+    CG_TRY(check_cuda(p, plan_malloc(&B.tile_rank, sizeof(int2) * capM), "cudaMalloc bins"));
+    CG_TRY(check_cuda(p, plan_malloc(&B.fperm, elem_bytes(p) * capM), "cudaMalloc bins"));
+    CG_TRY(check_cuda(p, plan_malloc(&B.count, sizeof(int32_t) * (capT + 1)), "cudaMalloc bins"));
+    CG_TRY(check_cuda(p, plan_malloc(&B.tile_off, sizeof(int32_t) * (capT + 1)), "cudaMalloc bins"));
+    CG_TRY(check_cuda(p, plan_malloc(&B.item_off, sizeof(int32_t) * (capT + 1)), "cudaMalloc bins"));
     const int64_t cap_items = capT + capM / std::max(1, p->tl.chunk) + 1;
-    CG_TRY(check_cuda(p, cudaMalloc(&B.items, sizeof(int4) * cap_items), "cudaMalloc bins"));
+    CG_TRY(check_cuda(p, plan_malloc(&B.items, sizeof(int4) * cap_items), "cudaMalloc bins"));
     B.max_items = cap_items;
     p->bins_capacity_M = capM;
     p->bins_capacity_tiles = capT;
@@ -560,6 +584,7 @@ int plan_forward(Plan* p, const void* fhat, void* f) {
   if (!p->nodes_set) return set_status(p, CUNFFT_X_NODES_NOT_SET, "forward: nodes not set");
   if (!p->bins.valid) CG_TRY(rebin(p));
   CG_TRY(prepare_interp(p));
+  if (p->timing) p->last_dir = 0;
   rec(p, 0);
   CG_TRY(check_cuda(p, launch_roc_forward(*p, fhat, p->g, p->stream), "roll-off kernel"));
   rec(p, 1);
@@ -573,6 +598,7 @@ int plan_forward(Plan* p, const void* fhat, void* f) {
 int plan_adjoint(Plan* p, const void* f, void* fhat) {
   if (!p->nodes_set) return set_status(p, CUNFFT_X_NODES_NOT_SET, "adjoint: nodes not set");
   if (!p->bins.valid) CG_TRY(rebin(p));
+  if (p->timing) p->last_dir = 1;
   rec(p, 0);
   CG_TRY(check_cuda(p, cudaMemsetAsync(p->g, 0, elem_bytes(p) * p->geo.ntot * p->geo.batch, p->stream),
                     "clear grid"));
@@ -682,7 +708,7 @@ int plan_autotune(Plan* p, int reps) {
   int best_sk = 0, best_ik = 0;
   const size_t bytes = elem_bytes(p);
   void* scratch_f = nullptr;
-  if (check_cuda(p, cudaMalloc(&scratch_f, bytes * std::max<int64_t>(p->M, 1)), "autotune scratch")) return p->last_status;
+  if (check_cuda(p, plan_malloc(&scratch_f, bytes * std::max<int64_t>(p->M, 1)), "autotune scratch")) return p->last_status;
   // non-zero data so that the spreading flush does real work while timed
   cudaMemsetAsync(scratch_f, 0x3c, bytes * std::max<int64_t>(p->M, 1), p->stream);
   cudaMemsetAsync(p->g, 0x3c, bytes * p->geo.ntot * p->geo.batch, p->stream);

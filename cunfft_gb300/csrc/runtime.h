@@ -54,6 +54,7 @@ struct Plan {
   // per-stage timing of the last call (seconds), recorded with events on the plan stream
   cudaEvent_t ev[8] = {};
   bool timing = false;
+  int last_dir = 0;       // direction of the last timed transform: 0 forward, 1 adjoint
   double t_bin = 0, t_roc = 0, t_fft = 0, t_conv = 0;
   // CUDA graphs of the forward [0] and adjoint [1] stage sequences
   cudaGraphExec_t gexec[2] = {nullptr, nullptr};
@@ -82,6 +83,18 @@ int plan_set_window(Plan* p, int window);
     int _s = (expr);                          \
     if (_s != CUNFFT_X_SUCCESS) return _s;    \
   } while (0)
+
+// Device allocation of the runtime (every cudaMalloc of the plans goes through it).
+// Host-side fault injection for the error-path tests: with CUNFFT_X_FAULT_ALLOC=k in
+// the environment the k-th call in the process (counted from 1) fails as an
+// out-of-memory cudaMalloc would, without touching the device; unset, it is cudaMalloc.
+cudaError_t plan_malloc(void** ptr, size_t bytes);
+template <typename T>
+inline cudaError_t plan_malloc(T** ptr, size_t bytes) {
+  return plan_malloc(reinterpret_cast<void**>(ptr), bytes);
+}
+// The same for the cuFFT plan creation: CUNFFT_X_FAULT_CUFFT=k fails the k-th one.
+bool plan_fft_fault();
 
 // status helpers
 int set_status(Plan* p, int code, const char* fmt, ...);

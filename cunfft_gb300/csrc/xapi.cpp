@@ -187,13 +187,15 @@ int cunfft_x_stage_times(cunfft_x_plan* h, double* t_bin, double* t_roc, double*
   if (!h) return CUNFFT_X_INVALID_ARGUMENT;
   cg::Plan& p = h->p;
   if (cudaStreamSynchronize(p.stream) != cudaSuccess) return CUNFFT_X_CUDA_ERROR;
-  // forward records 0 roc 1 fft 2 conv 3; adjoint records 0 conv 1 fft 2 roc 3
+  // forward records 0 roc 1 fft 2 conv 3; adjoint records 0 conv 1 fft 2 roc 3 (the
+  // reference's adjoint runs gridding, FFT, roll-off: src/cunfft.cu:209-224)
   const double s01 = ev_seconds(p.ev[0], p.ev[1]), s12 = ev_seconds(p.ev[1], p.ev[2]),
                s23 = ev_seconds(p.ev[2], p.ev[3]);
+  const bool adj = p.last_dir == 1;
   if (t_bin) *t_bin = ev_seconds(p.ev[6], p.ev[7]);
   if (t_fft) *t_fft = s12;
-  if (t_roc) *t_roc = s01;
-  if (t_conv) *t_conv = s23;
+  if (t_roc) *t_roc = adj ? s23 : s01;
+  if (t_conv) *t_conv = adj ? s01 : s23;
   return CUNFFT_X_SUCCESS;
 }
 

@@ -130,29 +130,41 @@ int cunfft_x_spread(cunfft_x_plan *plan, const void *f, void *g);
 
 /** Spreading without any memory allocation (no counterpart in the reference).
  *
- *  For callers that cannot allocate device memory: work recorded into a CUDA
- *  graph by stream capture (cudaMalloc cannot be captured), frameworks whose
- *  device memory all belongs to their own pool allocator, and real-time loops
- *  that must not pay for or fail on an allocation.  Same result as
- *  cunfft_x_spread on a one-instance plan with these parameters: g += spread of
- *  the samples f at the nodes x, where g is the caller's oversampled grid
- *  (prod n complex values of the given precision; clear it first for a fresh
- *  result), x holds M*d doubles and f M complex values, all device pointers,
- *  asynchronous on `stream` (NULL: the legacy default stream).  n may be NULL
- *  (n_t = 2*next_pow2(N_t)).
+ *  For callers that cannot allocate device memory: frameworks whose device memory
+ *  all belongs to their own pool allocator, real-time loops that must not pay for or
+ *  fail on an allocation mid-run, and host applications that forbid allocation in
+ *  their plug-in callbacks.  Same result as cunfft_x_spread on a one-instance plan
+ *  with these parameters: g += spread of the samples f at the nodes x, where g is
+ *  the caller's oversampled grid (prod n complex values of the given precision;
+ *  clear it first for a fresh result), x holds M*d doubles and f M complex values,
+ *  all device pointers, asynchronous on `stream` (NULL: the legacy default stream).
+ *  n may be NULL (n_t = 2*next_pow2(N_t)).  The Gaussian window only.
+ *
+ *  status: NULL, or a device pointer to one int32 that the call clears on the
+ *  stream and that holds, once the spreading has finished, 0 or a non-zero code
+ *  when a device-side check failed (a bounded completion wait of the tensor-core
+ *  kernel gave up; g is then incomplete).  Read it after synchronising the stream.
+ *  With NULL such a failure is not reported.
  *
  *  Its scratch (node bins, tile counts, work queue) is one fixed device array
  *  inside the library, about 58 MB, which every GPU that loads the library holds
  *  until the process exits.  Limits: M <= 1048576 nodes and at most 65536 grid
- *  tiles (every 3D grid up to 256^3 and every 2D grid up to 8192^2 fits); larger
- *  requests return
- *  CUNFFT_X_INVALID_ARGUMENT with a message on stderr.  The first call on each
- *  device looks up the array's device address; make that first call outside
- *  any stream capture.  All calls share the array: calls that overlap on the
- *  GPU (other streams, other host threads on the same device) race and must be
- *  serialised by the caller. */
+ *  tiles, the tiles being prod_t ceil(n_t / T_t) for the plan's default tile
+ *  extents T.  With m <= 7, 3D tiles are 8 x 8 x 16 (FP32) or 4 x 8 x 16 (FP64), so
+ *  n = 256^3 needs 16384 or 32768 tiles and fits, n = 512^3 does not; wider windows
+ *  (m >= 8) use 8 x 4 x 8 (FP32) or 4 x 4 x 8 (FP64) tiles in 3D, and a tile whose
+ *  padded copy would not fit shared memory is halved along dimension 0.  2D tiles
+ *  are 32 x 64 grid points, 1D tiles 2048.
+ *  Larger requests return CUNFFT_X_INVALID_ARGUMENT with a message on stderr and
+ *  do no device work.  M = 0 leaves g unchanged.
+ *
+ *  The first call on each device looks up the array's device address
+ *  (cudaGetSymbolAddress) and caches it: make that first call before any stream
+ *  capture, and do not use the entry point across a device reset.  All calls share
+ *  the array: calls that overlap on the GPU (other streams, other host threads on
+ *  the same device) race and must be serialised by the caller. */
 int cunfft_x_spread_noalloc(int d, const int64_t *N, const int64_t *n, int m, int precision, int64_t M,
-                            const double *x, const void *f, void *g, void *stream);
+                            const double *x, const void *f, void *g, void *stream, int32_t *status);
 
 /** Stream used by the plan (cudaStream_t as void*). */
 int cunfft_x_set_stream(cunfft_x_plan *plan, void *stream);
@@ -208,7 +220,10 @@ int cunfft_x_set_interp_kernel(cunfft_x_plan *plan, int kind);
 int cunfft_x_get_interp_kernel(const cunfft_x_plan *plan, int *kind);
 
 /** Per-stage device times of the last forward/adjoint call, in seconds
- *  (binning, roll-off, FFT, gridding).  Blocks until the plan stream is idle. */
+ *  (binning, roll-off, FFT, gridding), by stage whatever the direction: after an
+ *  adjoint, t_conv is the spreading and t_roc the crop (the reference fills
+ *  CUNFFTTimes the same way, src/cunfft.cu:209-224).  Blocks until the plan stream
+ *  is idle. */
 int cunfft_x_stage_times(cunfft_x_plan *plan, double *t_bin, double *t_roc, double *t_fft, double *t_conv);
 
 /** Forward transform between host buffers, with the copies on the plan's two copy

@@ -73,8 +73,9 @@ def parse(ref_root):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    kats = parse(ref)
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_kats.py <path of the CUNFFT source tree>")
+    kats = parse(sys.argv[1])
     out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "kats.json")
     with open(out, "w") as fh:
         json.dump({"source": "sukunis/CUNFFT Tests/Runtime logs (E_inf CUNDFT vs CUNFFT column)",

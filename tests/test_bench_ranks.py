@@ -48,8 +48,8 @@ def test_gloo_two_ranks_max_time_and_job_value():
 
 def test_reference_arm_nonzero_rank_exits_quietly():
     env = dict(os.environ, RANK="1", WORLD_SIZE="2", LOCAL_RANK="1")
-    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
-                        "--warmup", "0"], env=env, capture_output=True, text=True, timeout=120)
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--gpus", "2",
+                        "--steps", "1", "--warmup", "0"], env=env, capture_output=True, text=True, timeout=120)
     assert r.returncode == 0 and r.stdout.strip() == ""
 
 
@@ -59,3 +59,12 @@ def test_single_rank_value_formula():
     assert bench.max_over_ranks_on(7.0, 1, None) == 7.0
     assert bench.replica_points_per_s(1000, 1, 1.0) == pytest.approx(1e6)
     json.dumps({"metric": bench.METRIC, "unit": bench.UNIT})
+
+
+def test_gpus_flag_must_match_the_launcher():
+    """--gpus N under a launcher that started a different number of ranks fails loudly
+    instead of timing fewer GPUs than asked for."""
+    env = dict(os.environ, RANK="0", WORLD_SIZE="1", LOCAL_RANK="0")
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--gpus", "2", "--steps", "1"], env=env,
+                       capture_output=True, text=True, timeout=120)
+    assert r.returncode == 2 and "WORLD_SIZE=1" in r.stderr

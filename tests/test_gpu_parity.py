@@ -404,3 +404,40 @@ def test_errors_are_status_codes(dev):
         p.forward(torch.zeros(16, dtype=torch.complex128, device=dev))
     assert ei.value.status == nat.NODES_NOT_SET
     p.close()
+
+
+def test_stage_times_name_stages_in_both_directions(dev):
+    """cunfft_x_stage_times reports by stage, not by position: after a forward and after
+    an adjoint, `conv` holds the gridding time and `roc` the roll-off (the reference's
+    adjoint runs gridding, FFT and roll-off in that order, src/cunfft.cu:209-224).  With
+    2^20 nodes on a 64^3 grid the gridding dwarfs the roll-off of 32^3 coefficients."""
+    from cunfft_gb300.nfft import NFFT
+
+    rng = np.random.default_rng(47)
+    N, M = [32, 32, 32], 1 << 20
+    x = torch.from_numpy(rng.uniform(-0.5, 0.5, (M, 3))).to(dev)
+    fh = torch.from_numpy(_rand(N, rng)).to(dev, torch.complex64)
+    f = torch.from_numpy(_rand(M, rng)).to(dev, torch.complex64)
+    p = NFFT(N, precision="f32", device=dev).set_nodes(x)
+    out_f = torch.empty(M, dtype=torch.complex64, device=dev)
+    out_h = torch.empty(N, dtype=torch.complex64, device=dev)
+    for _ in range(2):  # warm-up: first launches set kernel attributes
+        p.forward(fh, out=out_f)
+        p.adjoint(f, out=out_h)
+    p.forward(fh, out=out_f)
+    st_f = p.stage_times()
+    p.adjoint(f, out=out_h)
+    st_a = p.stage_times()
+    # the gridding stages alone, timed with events on the plan's stream
+    grid = torch.zeros_like(p.grid())
+    s = torch.cuda.current_stream(dev)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(s)
+    p.spread(f, grid)
+    b.record(s)
+    b.synchronize()
+    t_spread = a.elapsed_time(b) * 1e-3
+    assert st_f["conv"] > 4 * st_f["roc"], st_f
+    assert st_a["conv"] > 4 * st_a["roc"], st_a
+    assert 0.3 * t_spread < st_a["conv"] < 3.0 * t_spread + 1e-4, (st_a, t_spread)
+    p.close()
