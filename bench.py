@@ -438,6 +438,21 @@ def run_ours(args):
     # samples, all 128^3 coefficients): the FP32 kernels' own error, which the window
     # error against the NDFT (about 1e-6 at m = 6) would hide
     err_form = {"forward": rel_l2(o64f, r32f), "adjoint": rel_l2(o64h, r32h_full)}
+    # the gridding kernels alone, FP32 against FP64 on identical inputs: interpolation of
+    # the FP64 forward's post-FFT grid (rounded to c64 for the FP32 kernel), spreading of
+    # the samples into a cleared grid; no FFT, roll-off or input rounding in between
+    p64.set_nodes(x)
+    p64.forward(fh64, out=o64f)
+    g64 = p64.grid().clone()
+    i64 = p64.interp(g64)
+    i32 = p32.interp(g64.to(torch.complex64))
+    s64 = p64.spread(f64)
+    s32 = p32.spread(f32)
+    err_grid = {"interp": rel_l2(i64, i32), "spread": rel_l2(s64, s32),
+                "note": "FP32 tensor-core gridding (FP16 hi/lo x3, FP32 accumulate) against the FP64 gridding on "
+                        "the same nodes, grid and samples: the kernels' own error"}
+    del g64, i64, i32, s64, s32
+    p64.forward(fh64, out=o64f)
     sub.close()
 
     # ---------------- ES window (cunfft_x_set_window): same step, same NDFT subsamples ----------------
@@ -530,6 +545,7 @@ def run_ours(args):
         "es_window": es,
         "rel_l2_vs_ndft": err,
         "rel_l2_fp32_vs_fp64_form": err_form,
+        "rel_l2_fp32_vs_fp64_gridding": err_grid,
         "stages_fp32": stages32,
         "e2e": {"value": replica_points_per_s(M, world, ms_e2e), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": ms_e2e,

@@ -6,7 +6,8 @@
 namespace cg {
 
 bool spread_tc_supported(const Plan& p) {
-  return p.prec == kF32 && !p.tl.use_global && spread_tc_ok(p.geo.d, p.geo.W, p.tl.T[0]);
+  return (p.prec == kF32 && !p.tl.use_global && spread_tc_ok(p.geo.d, p.geo.W, p.tl.T[0])) ||
+         spread2_tm_supported(p);
 }
 
 // Dynamic shared memory of one CTA.  Besides the kernel's own needs it is large
@@ -66,6 +67,7 @@ static cudaError_t launch_tc(const Plan& p, const void* in, void* out, cudaStrea
 }
 
 cudaError_t grid_launch_spread_tc(const Plan& p, const void* in, void* out, cudaStream_t st) {
+  if (p.geo.d == 2) return grid_launch_spread2_tm(p, in, out, st);
   if (spread_tm_supported(p)) return grid_launch_spread_tm(p, in, out, st);
   switch (p.geo.W) {
     case 4: return launch_tc<4>(p, in, out, st);

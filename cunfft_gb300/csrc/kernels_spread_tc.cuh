@@ -132,6 +132,16 @@ __device__ __forceinline__ void tc_split8_f16(const float* v, uint4& hi, uint4& 
   lo = make_uint4(l[0], l[1], l[2], l[3]);
 }
 
+// 2 FP32 values -> FP16 hi pair and lo = fp16(v - hi) pair (the subtraction as one
+// packed FP32 add)
+__device__ __forceinline__ void tc_split2_f16(float2 v, uint32_t& hi, uint32_t& lo) {
+  const __half2 hh = __float22half2_rn(v);
+  const float2 hf = __half22float2(hh);
+  const __half2 ll = __float22half2_rn(__fadd2_rn(v, make_float2(-hf.x, -hf.y)));
+  hi = *reinterpret_cast<const uint32_t*>(&hh);
+  lo = *reinterpret_cast<const uint32_t*>(&ll);
+}
+
 // 4 FP32 values -> FP16 hi (4 halves) and lo = fp16(v - hi) (4 halves)
 __device__ __forceinline__ void tc_split4_f16(const float* v, uint2& hi, uint2& lo) {
   uint32_t h[2], l[2];

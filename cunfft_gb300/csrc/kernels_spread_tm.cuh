@@ -24,7 +24,8 @@
 // Warp roles (20 warps): 15 builders, one MMA issuer (lane 0), 4 epilogue warps.  Per
 // batch the builders (1) evaluate w0 / w1 over the tile's planes and rows (lane = node
 // and dimension) and the B values w2 f (lane = node and column) into shared tables
-// (warps 8-14), then after a named barrier among themselves (2) write A
+// (warps 8-14; w1 pre-scaled by the A scale 2^10), then after a named barrier among
+// themselves (2) write A
 // (warps 0-7: warp w owns lane quarter w % 4 of M-tiles w / 4 and w / 4 + 2) and split
 // B into its shared-memory stage (warps 8-14).  The epilogue copies each M-tile into
 // shared staging rows and releases it before its atomics.  Hand-offs are mbarriers; every wait
@@ -209,8 +210,9 @@ __global__ void __launch_bounds__(kTmThreads, 1) k_spread_tm(const float2* __res
           const int o = hd ? (int)((off >> SH) & MASK) : (int)(off & MASK);
           const int Ed = hd ? E1 : E0;
           const TapK kd = hd ? k1 : k0;
+          const float sc = hd ? kTcScaleA : 1.f;  // w1 carries the A scale 2^10
           float* const col = wx + (hd ? E0 : 0) * kTcWxStride + j;
-          for (int p = bw; p < Ed; p += kTmBWarps) col[p * kTcWxStride] = tc_tap<WIN>(fr, mf, p - o, W, kd);
+          for (int p = bw; p < Ed; p += kTmBWarps) col[p * kTcWxStride] = tc_tap<WIN>(fr, mf, p - o, W, kd) * sc;
         }
         const int o2 = (int)(off >> (2 * SH));
         const float fr2 = frac[j * 3 + 2];
@@ -233,21 +235,19 @@ __global__ void __launch_bounds__(kTmThreads, 1) k_spread_tm(const float2* __res
         break;
       }
       if (warp < kTmAWarps) {
-        // (2) A rows of lane aL, M-tiles amt and amt + 2: w0 w1 2^10 -> FP16 hi, lo
+        // (2) A rows of lane aL, M-tiles amt and amt + 2: w0 (w1 2^10) -> FP16 hi, lo
         tc::fence_after_sync();
-        float w1r[kTcK];
+        float2 w1r[kTcK / 2];
         if (a_row) {
 #pragma unroll
           for (int c4 = 0; c4 < kTcK / 4; ++c4) {
             const float4 t = *reinterpret_cast<const float4*>(wx + (E0 + ap1) * kTcWxStride + 4 * c4);
-            w1r[4 * c4] = t.x * kTcScaleA;
-            w1r[4 * c4 + 1] = t.y * kTcScaleA;
-            w1r[4 * c4 + 2] = t.z * kTcScaleA;
-            w1r[4 * c4 + 3] = t.w * kTcScaleA;
+            w1r[2 * c4] = make_float2(t.x, t.y);
+            w1r[2 * c4 + 1] = make_float2(t.z, t.w);
           }
         } else {
 #pragma unroll
-          for (int k = 0; k < kTcK; ++k) w1r[k] = 0.f;
+          for (int k = 0; k < kTcK / 2; ++k) w1r[k] = make_float2(0.f, 0.f);
         }
         const uint32_t tq = tmem + ((uint32_t)(32 * aq) << 16) + kTmACol0 + st * kTmAStageCols;
 #pragma unroll
@@ -255,28 +255,17 @@ __global__ void __launch_bounds__(kTmThreads, 1) k_spread_tm(const float2* __res
           const int mt = amt + 2 * i;
           if (mt < L.mt) {
             const int p0 = aa + AP * mt;
-            float v[kTcK];
+            uint32_t hi[8], lo[8];
             if (a_row && p0 < E0) {
 #pragma unroll
               for (int c4 = 0; c4 < kTcK / 4; ++c4) {
                 const float4 t = *reinterpret_cast<const float4*>(wx + p0 * kTcWxStride + 4 * c4);
-                v[4 * c4] = t.x * w1r[4 * c4];
-                v[4 * c4 + 1] = t.y * w1r[4 * c4 + 1];
-                v[4 * c4 + 2] = t.z * w1r[4 * c4 + 2];
-                v[4 * c4 + 3] = t.w * w1r[4 * c4 + 3];
+                tc_split2_f16(__fmul2_rn(make_float2(t.x, t.y), w1r[2 * c4]), hi[2 * c4], lo[2 * c4]);
+                tc_split2_f16(__fmul2_rn(make_float2(t.z, t.w), w1r[2 * c4 + 1]), hi[2 * c4 + 1], lo[2 * c4 + 1]);
               }
             } else {
 #pragma unroll
-              for (int k = 0; k < kTcK; ++k) v[k] = 0.f;
-            }
-            uint32_t hi[8], lo[8];
-#pragma unroll
-            for (int c = 0; c < 8; ++c) {
-              const __half2 hh = __floats2half2_rn(v[2 * c], v[2 * c + 1]);
-              const float2 hf = __half22float2(hh);
-              const __half2 ll = __floats2half2_rn(v[2 * c] - hf.x, v[2 * c + 1] - hf.y);
-              hi[c] = *reinterpret_cast<const uint32_t*>(&hh);
-              lo[c] = *reinterpret_cast<const uint32_t*>(&ll);
+              for (int c = 0; c < 8; ++c) hi[c] = lo[c] = 0u;
             }
             tc::tmem_st8(tq + (uint32_t)(16 * mt), hi);
             tc::tmem_st8(tq + (uint32_t)(16 * mt + 8), lo);

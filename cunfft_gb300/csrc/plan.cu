@@ -93,7 +93,9 @@ static void free_bins(Plan* p) {
 // FP32 3D tiles (8 x 8 x 16) leave room for two CTAs per SM.
 static void default_tiles(const Plan* p, int* T) {
   const int d = p->geo.d, W = p->geo.W;
-  T[0] = d == 1 ? 2048 : (d == 2 ? 32 : (p->prec == kF32 ? 8 : 4));
+  // 2D FP32 with 2m+2 <= 16: 64 x 64 tiles, the largest the tensor-core spreading covers
+  // (E0 = 63 + W rows of its 128-row MMA)
+  T[0] = d == 1 ? 2048 : (d == 2 ? (p->prec == kF32 && W <= 16 ? 64 : 32) : (p->prec == kF32 ? 8 : 4));
   if (d == 2) T[1] = fixed_t_last(2, W);
   if (d == 3) {
     T[1] = fixed_t_mid(3, W);

@@ -142,6 +142,9 @@ cudaError_t launch_wait_gives_up(int32_t* status, cudaStream_t st);
 // tensor form runs it whenever the tile's planes fit its four M-tiles
 bool spread_tm_supported(const Plan& p);
 cudaError_t grid_launch_spread_tm(const Plan& p, const void* f, void* g, cudaStream_t st);
+// 2D tensor-core spreading kernel (grid_spread2_tm.cu); the tensor form runs it for 2D plans
+bool spread2_tm_supported(const Plan& p);
+cudaError_t grid_launch_spread2_tm(const Plan& p, const void* f, void* g, cudaStream_t st);
 // tensor-core interpolation kernel (grid_interp_tc.cu)
 bool interp_tc_supported(const Plan& p);
 cudaError_t grid_launch_interp_tc(const Plan& p, const void* g, void* f, cudaStream_t st);

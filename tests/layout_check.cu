@@ -5,6 +5,7 @@
 #include <cstdio>
 
 #include "kernels_interp_tc.cuh"
+#include "kernels_spread2_tm.cuh"
 #include "kernels_spread_tm.cuh"
 
 using namespace cg;
@@ -47,6 +48,19 @@ int main() {
         CHECK(L.dyn <= kMaxSmem, "interp W %d T0 %d: shared %u", W, T0, L.dyn);
         CHECK(it_pairs(W) <= kItHalf && it_ch(W) >= 1, "interp W %d T0 %d: chunk", W, T0);
       }
+    }
+  }
+  {
+    const T2Layout L = t2_layout();
+    CHECK(L.total <= kMaxSmem, "spread2: shared %u", L.total);
+    CHECK(L.rec_off % 16 == 0 && L.tab_off % 16 == 0 && L.tab_bytes % 16 == 0 && L.bar_off % 16 == 0 &&
+              L.stg_off % 16 == 0 && (kT2StgStride * 4) % 16 == 0,
+          "spread2: align");
+    CHECK(kT2ACol0 + kT2Stages * 16u <= 512u, "spread2: tmem");
+    for (int W = 4; W <= 16; W += 2) {
+      CHECK(2 * (64 + W - 1) <= kT2N && kT2MaxT0 + W - 1 <= 128, "spread2 W %d: extents", W);
+      // table reads: row p0 < 128 or column p1 < 80 of a node with window start 0 <= o < 64
+      CHECK(kT2Zero + 127 <= kT2Pad - 1 && kT2Zero - 63 >= 0 && kT2Zero + W <= kT2Pad, "spread2 W %d: table rows", W);
     }
   }
   std::printf("layout check: %d failures\n", fails);
