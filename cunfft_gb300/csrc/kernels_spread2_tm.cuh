@@ -371,8 +371,9 @@ __global__ void __launch_bounds__(kT2Threads, 1) k_spread2_tm(const float2* __re
       }
       tc::bulk_wait_read();  // the previous item's reductions have read this thread's row
       tc::fence_after_sync();
-      const bool row = ep0 < E0;
-      if (row) {
+      // tcgen05.ld is warp-collective: a warp with any tile row reads all 32 of its lanes
+      // (the rows past E0 are zeros, staged and never reduced)
+      if (32 * q < E0) {
         const uint32_t acc = tmem + set * kT2N + ((uint32_t)(32 * q) << 16);
 #pragma unroll
         for (int c = 0; c < kT2N / 16; ++c) {
@@ -387,39 +388,41 @@ __global__ void __launch_bounds__(kT2Threads, 1) k_spread2_tm(const float2* __re
       }
       tc::fence_before_sync();
       tc::mbar_arrive_warp(&acc_empty[set]);
-      if (!row) continue;
-      const TileOrigin o = decode_tile<2>(geo, tl, item.x);
-      float2* const rowa = g + o.inst * geo.ntot + wrap_up(o.a[0] + ep0, n0) * n1;  // grid row start
-      const int kw = (int)(n1 - o.a[1] < 128 ? n1 - o.a[1] : 128);  // columns before the row end (capped > E1)
-      if (one_wrap && (n1 & 1) == 0) {
-        // run 1: columns [0, c1) at a1 + p1; run 2: columns [kw, E1) at p1 - kw (wrapped)
-        tc::fence_proxy_async_smem();  // staged row -> bulk-copy engine
-        const uint32_t s0 = tc::smem_u32(srow);
-        const int c1 = E1 < kw ? E1 : kw;
-        const uint32_t b1 = (uint32_t)((c1 + 1) & ~1) * 8u;
-        const uint32_t b2 = kw < E1 ? (uint32_t)((E1 - kw + 1) & ~1) * 8u : 0u;
-        float2* const dst1 = rowa + o.a[1];
-        const bool aligned = ((reinterpret_cast<uintptr_t>(dst1) | s0) & 15u) == 0u &&
-                             ((reinterpret_cast<uintptr_t>(rowa) | (s0 + (uint32_t)kw * 8u)) & 15u) == 0u;
-        if (aligned) {
-          tc::bulk_reduce_add_f32(dst1, s0, b1);
-          if (b2) tc::bulk_reduce_add_f32(rowa, s0 + (uint32_t)kw * 8u, b2);
-          tc::bulk_commit();
-          continue;
+      if (ep0 < E0) {
+        const TileOrigin o = decode_tile<2>(geo, tl, item.x);
+        float2* const rowa = g + o.inst * geo.ntot + wrap_up(o.a[0] + ep0, n0) * n1;  // grid row start
+        const int kw = (int)(n1 - o.a[1] < 128 ? n1 - o.a[1] : 128);  // columns before the row end (capped > E1)
+        bool done = false;
+        if (one_wrap && (n1 & 1) == 0) {
+          // run 1: columns [0, c1) at a1 + p1; run 2: columns [kw, E1) at p1 - kw (wrapped)
+          tc::fence_proxy_async_smem();  // staged row -> bulk-copy engine
+          const uint32_t s0 = tc::smem_u32(srow);
+          const int c1 = E1 < kw ? E1 : kw;
+          const uint32_t b1 = (uint32_t)((c1 + 1) & ~1) * 8u;
+          const uint32_t b2 = kw < E1 ? (uint32_t)((E1 - kw + 1) & ~1) * 8u : 0u;
+          float2* const dst1 = rowa + o.a[1];
+          done = ((reinterpret_cast<uintptr_t>(dst1) | s0) & 15u) == 0u &&
+                 ((reinterpret_cast<uintptr_t>(rowa) | (s0 + (uint32_t)kw * 8u)) & 15u) == 0u;
+          if (done) {
+            tc::bulk_reduce_add_f32(dst1, s0, b1);
+            if (b2) tc::bulk_reduce_add_f32(rowa, s0 + (uint32_t)kw * 8u, b2);
+            tc::bulk_commit();
+          }
+        }
+        for (int p = 0; p < E1 && !done; p += 2) {
+          const float4 w = *reinterpret_cast<const float4*>(srow + 2 * p);
+          const int64_t c0 = wrap_up(o.a[1] + p, n1);
+          if (p + 1 < E1 && pairs && c0 + 1 < n1) {  // pair (p, p + 1) 16-byte aligned and not split by the wrap
+            if (w.x != 0.f || w.y != 0.f || w.z != 0.f || w.w != 0.f)
+              atomicAdd(reinterpret_cast<float4*>(rowa + c0), w);
+          } else {
+            if (w.x != 0.f || w.y != 0.f) atomicAdd(rowa + c0, make_float2(w.x, w.y));
+            if (p + 1 < E1 && (w.z != 0.f || w.w != 0.f))
+              atomicAdd(rowa + wrap_up(o.a[1] + p + 1, n1), make_float2(w.z, w.w));
+          }
         }
       }
-      for (int p = 0; p < E1; p += 2) {
-        const float4 w = *reinterpret_cast<const float4*>(srow + 2 * p);
-        const int64_t c0 = wrap_up(o.a[1] + p, n1);
-        if (p + 1 < E1 && pairs && c0 + 1 < n1) {  // pair (p, p + 1) 16-byte aligned and not split by the wrap
-          if (w.x != 0.f || w.y != 0.f || w.z != 0.f || w.w != 0.f)
-            atomicAdd(reinterpret_cast<float4*>(rowa + c0), w);
-        } else {
-          if (w.x != 0.f || w.y != 0.f) atomicAdd(rowa + c0, make_float2(w.x, w.y));
-          if (p + 1 < E1 && (w.z != 0.f || w.w != 0.f))
-            atomicAdd(rowa + wrap_up(o.a[1] + p + 1, n1), make_float2(w.z, w.w));
-        }
-      }
+      __syncwarp();  // the warp reconverges before the next item's collective TMEM reads
     }
     tc::bulk_wait_all();  // every reduction complete before the CTA's shared memory goes
   }

@@ -225,7 +225,8 @@ int plan_set_spread_kernel(Plan* p, int kind) {
                       "register spreading needs d = 3, FP32, 2m+2 <= 16 and an outer tile extent <= 8");
   if (kind == CUNFFT_X_SPREAD_TENSOR && !spread_tc_supported(*p))
     return set_status(p, CUNFFT_X_UNSUPPORTED,
-                      "tensor-core spreading needs d = 3, FP32, 2m+2 <= 16 and an outer tile extent <= 16");
+                      "tensor-core spreading needs FP32, 2m+2 <= 16 and d = 3 with an outer tile extent <= 16 "
+                      "or d = 2 with tile extents <= 64");
   p->spread_mode = kind;
   p->tl.spread_kernel = pick_spread_kernel(*p, kind);
   ++p->node_gen;

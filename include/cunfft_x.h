@@ -29,15 +29,15 @@ extern "C" {
 enum { CUNFFT_X_F64 = 0, CUNFFT_X_F32 = 1 };
 
 /** Spreading (adjoint gridding) kernel.  AUTO picks TENSOR where it applies
- *  (d = 3, FP32, 2m+2 <= 16, outer tile extent <= 16), else REGISTER (same, outer
- *  tile extent <= 8), else SHARED; GLOBAL is reported when no shared-memory tile
- *  fits (wide 3D windows). */
+ *  (FP32, 2m+2 <= 16, and d = 3 with outer tile extent <= 16 or d = 2 with tile
+ *  extents <= 64), else REGISTER (d = 3, FP32, 2m+2 <= 16, outer tile extent <= 8),
+ *  else SHARED; GLOBAL is reported when no shared-memory tile fits (wide 3D windows). */
 enum {
   CUNFFT_X_SPREAD_AUTO = 0,
   CUNFFT_X_SPREAD_SHARED = 1,   /* padded tile in shared memory, warp-owned planes */
   CUNFFT_X_SPREAD_REGISTER = 2, /* padded tile in registers, one warp per plane */
   CUNFFT_X_SPREAD_GLOBAL = 3,   /* atomics straight into the grid (fallback) */
-  CUNFFT_X_SPREAD_TENSOR = 4    /* tile update as 3xTF32 tcgen05 MMAs, tile in tensor memory */
+  CUNFFT_X_SPREAD_TENSOR = 4    /* tile update as FP16 hi/lo x3 tcgen05 MMAs, tile in tensor memory */
 };
 
 /** Interpolation (forward gridding) kernel.  AUTO picks TENSOR where it applies
@@ -47,7 +47,7 @@ enum {
   CUNFFT_X_INTERP_AUTO = 0,
   CUNFFT_X_INTERP_SHARED = 1,   /* tile staged in shared memory, warp per node */
   CUNFFT_X_INTERP_GLOBAL = 3,   /* taps read straight from the grid (fallback) */
-  CUNFFT_X_INTERP_TENSOR = 4    /* innermost contraction as 3xTF32 tcgen05 MMAs */
+  CUNFFT_X_INTERP_TENSOR = 4    /* innermost contraction as FP16 hi/lo x3 tcgen05 MMAs */
 };
 
 /** Status codes returned by every cunfft_x_* entry point. */
@@ -69,9 +69,9 @@ typedef struct cunfft_x_plan cunfft_x_plan;
  *  sizes, any n_t >= N_t (NULL selects n_t = 2*next_pow2(N_t) like cunfft_init,
  *  src/cunfft.cu:296-299).  The reference wraps window indices with &(n-1)
  *  (src/cunfft_kernel.cu:590, :768, :1036), so there n must be a power of two;
- *  here any size wraps correctly.  The tensor-core gridding forms need 3D with an
- *  even last size (spreading) or one divisible by 8 (interpolation); other
- *  sizes run the shared-tile forms.  1 <= m <= 15; precision CUNFFT_X_F64 or
+ *  here any size wraps correctly.  The 3D tensor-core gridding forms need an even
+ *  last size (spreading) or one divisible by 8 (interpolation), other sizes run the
+ *  shared-tile forms; the 2D tensor-core spreading takes any size.  1 <= m <= 15; precision CUNFFT_X_F64 or
  *  CUNFFT_X_F32; batch >= 1 instances; stream 0 creates a private stream
  *  (a cudaStream_t may be passed as void*). */
 int cunfft_x_plan_create(cunfft_x_plan **plan, int d, const int64_t *N, const int64_t *n, int m,

@@ -70,7 +70,7 @@ def test_spread2d_outer_tile_extents(dev, T0):
 
 
 @pytest.mark.parametrize("N,n", [([8, 8], None), ([4, 64], None), ([64, 4], None), ([33, 45], [70, 90]),
-                                 ([33, 45], [71, 91]), ([40, 100], [48, 102])])
+                                 ([33, 45], [71, 91]), ([40, 100], [80, 202])])
 def test_spread2d_small_odd_and_general_grids(dev, N, n):
     """Rows shorter than the padded tile (the columns wrap more than once), odd row lengths
     and odd or non-power-of-two grid sizes take the kernel's atomic paths."""

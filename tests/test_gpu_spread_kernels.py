@@ -166,15 +166,25 @@ def test_spread_kernel_selection_rules(dev):
     from cunfft_gb300._native import CunfftError
     from cunfft_gb300.nfft import NFFT
     x3 = torch.rand(100, 3, dtype=torch.float64, device=dev) - 0.5
-    # FP64 and 2D plans: only the shared-tile kernel
-    for prec, N, x in (("f64", [16, 16, 16], x3), ("f32", [32, 32], x3[:, :2].contiguous())):
-        p = NFFT(N, precision=prec, device=dev).set_nodes(x)
+    # FP64 plans and 2D plans with 2m+2 > 16: only the shared-tile kernel
+    for prec, N, x, m in (("f64", [16, 16, 16], x3, 6), ("f32", [32, 32], x3[:, :2].contiguous(), 8)):
+        p = NFFT(N, m=m, precision=prec, device=dev).set_nodes(x)
         assert p.spread_kernel() == "shared"
         for k in ("register", "tensor"):
             with pytest.raises(CunfftError):
                 p.set_spread_kernel(k)
         assert p.spread_kernel() == "shared"
         p.close()
+    # 2D FP32 with 2m+2 <= 16: the 2D tensor-core kernel (tiles up to 64 x 64), no register form
+    p = NFFT([128, 128], precision="f32", device=dev).set_nodes(x3[:, :2].contiguous())
+    assert p.spread_kernel() == "tensor"
+    with pytest.raises(CunfftError):
+        p.set_spread_kernel("register")
+    p.set_tiling([128])                 # beyond the kernel's 64-row outer extent: shared
+    assert p.spread_kernel() == "shared"
+    p.set_tiling([32])
+    assert p.spread_kernel() == "tensor"
+    p.close()
     # 2m+2 = 18 > 16
     p = NFFT([16, 16, 16], m=8, precision="f32", device=dev).set_nodes(x3)
     assert p.spread_kernel() == "shared"
