@@ -13,26 +13,26 @@
 // in the 3D kernels), both operands split into FP16 hi + lo and the three products
 // hi*hi + hi*lo + lo*hi accumulated in FP32 in tensor memory.
 //
-// Unlike 3D, both operands are one tap table wide: a node costs 128 A entries and 160 B
-// entries (against W^2 <= 256 taps), and the tensor core does the W^2 multiply-adds.  The
-// taps come from per-node tables in which tap l of a node sits at index kT2Zero + l of a
-// row of kT2Pad floats that is zero elsewhere, so the A thread of row p0 reads
-// w0[j][kT2Zero + p0 - o0_j] and the B thread of column p1 reads w1[j][kT2Zero + p1 - o1_j]
-// without a bounds test (rows and columns outside the window read zeros).
+// Unlike 3D, both operands are one tap wide: a node costs 128 A entries and 160 B entries
+// (against W^2 <= 256 taps), and the tensor core does the W^2 multiply-adds.  Each operand
+// thread evaluates the taps of its own row (A: row p0, w0 of the 16 nodes) or column pair
+// (B: column p1, w1 of 8 nodes) straight from the node records, so no stage sits between
+// the records and the operands.
 //
-// Warp roles (16 warps): A warps 0-3 (warp w writes TMEM lanes 32 w .. 32 w + 31, one row
-// p0 per thread, its hi and lo halves with tcgen05.st), B warps 4-8 (thread t of 160:
-// rows 2 p1 and 2 p1 + 1 of B, nodes 8 h .. 8 h + 7, p1 = t / 2, h = t % 2, into the
-// shared-memory operand stage), table warps 9-10 (node records through a cp.async ring,
-// then the taps of half the window each, lane = node and dimension), the MMA warp 11
-// (lane 0) and epilogue warps 12-15 (TMEM lane quarter warp % 4).  The table buffers are
-// double-buffered (tab_full / tab_empty), the operands four stages deep (full / empty),
-// the accumulators double-buffered in tensor memory (acc_full / acc_empty): while the
-// epilogue reads one work item's tile out and adds it to the grid as bulk FP32 reductions
-// (cp.reduce.async.bulk, one or two per row), the MMAs of the next item accumulate into
-// the other set.  Every mbarrier wait is bounded; a wait that gives up sets the plan's
-// device status flag, after which the kernel drains (bounded), frees its tensor memory and
-// returns.
+// Warp roles (25 warps): two sets of operand warps that take alternate batches (set s the
+// batches gb with gb % 2 = s), A warps 0-3 and 16-19 (warp w writes TMEM lanes
+// 32 (w % 4) .. + 31 of the operand stage, one row p0 per thread, hi and lo halves with
+// tcgen05.st), B warps 4-8 and 20-24 (thread t of 160: rows 2 p1 and 2 p1 + 1 of B, nodes
+// 8 h .. 8 h + 7, p1 = t / 2, h = t % 2, into the shared-memory operand stage); the record
+// warp 9 (node records into a ring of kT2Ring slots by cp.async, kT2Ahead batches ahead);
+// the MMA warp 10 (lane 0); epilogue warps 12-15 (TMEM lane quarter warp % 4); warp 11
+// idles.  Operands are four stages deep (full / empty), records kT2Ring deep (rec_full /
+// rec_empty), and the accumulators double-buffered in tensor memory (acc_full /
+// acc_empty): while the epilogue reads one work item's tile out and adds it to the grid as
+// bulk FP32 reductions (cp.reduce.async.bulk, one or two per row), the MMAs of the next
+// item accumulate into the other set.  Every mbarrier wait is bounded; a wait that gives up
+// sets the plan's device status flag, after which the kernel drains (bounded), frees its
+// tensor memory and returns.
 #pragma once
 
 #include <cuda_fp16.h>
@@ -45,13 +45,16 @@ constexpr int kT2MaxT0 = 64;               // E0 = T0 + W - 1 <= 128 rows (M = 1
 constexpr int kT2N = 160;                  // MMA N: 2 E1 <= 158 columns (p1, re|im), padded
 constexpr int kT2AWarps = 4;
 constexpr int kT2BWarps = 5;               // 160 threads: (p1 < 80, node half)
-constexpr int kT2TabWarp0 = kT2AWarps + kT2BWarps;  // warps 9, 10
-constexpr int kT2MmaWarp = kT2TabWarp0 + 2;         // warp 11
-constexpr int kT2EpiWarp0 = kT2MmaWarp + 1;         // warps 12-15: lane quarters 0-3
-constexpr int kT2Threads = (kT2EpiWarp0 + 4) * 32;
+constexpr int kT2OpWarps = kT2AWarps + kT2BWarps;
+constexpr int kT2RecWarp = kT2OpWarps;     // warp 9
+constexpr int kT2MmaWarp = kT2RecWarp + 1; // warp 10
+constexpr int kT2EpiWarp0 = 12;            // warps 12-15: lane quarters 0-3
+constexpr int kT2OpSet1 = 16;              // warps 16-24: the operand warps of odd batches
+constexpr int kT2Threads = (kT2OpSet1 + kT2OpWarps) * 32;
 constexpr int kT2Stages = 4;
-constexpr int kT2Pad = 193;                // floats per node and dimension in the tap tables (odd)
-constexpr int kT2Zero = 64;                // table index of tap 0 (p0 - o0 >= -63)
+constexpr int kT2Ring = 8;                 // record slots
+constexpr int kT2Ahead = 4;                // record loads in flight (batches)
+constexpr uint32_t kT2Spin = 64;           // non-blocking polls before a hand-off wait suspends
 constexpr uint32_t kT2BBytes = (uint32_t)kT2N * kTcK * 2u;   // one FP16 part of one B stage
 constexpr uint32_t kT2ACol0 = 2u * kT2N;   // A stages after the two accumulator sets
 constexpr int kT2StgStride = kT2N + 4;     // floats per staging row
@@ -64,10 +67,8 @@ __host__ __device__ constexpr bool spread2_tm_ok(int d, int W, int T0, int T1) {
 // Shared-memory layout of k_spread2_tm (byte offsets; host and device agree).
 struct T2Layout {
   uint32_t b_off;     // kT2Stages x (B hi, B lo)
-  uint32_t rec_off;   // kTcRing record slots
-  uint32_t tab_off;   // 2 x table buffer
-  uint32_t tab_bytes; // w0 [16][kT2Pad], w1 [16][kT2Pad] floats, then samples [16] float2, offsets [16] int2
-  uint32_t bar_off;   // full[4], empty[4], acc_full[2], acc_empty[2], tab_full[2], tab_empty[2];
+  uint32_t rec_off;   // kT2Ring record slots: window starts [16], fractions [16][2], samples [16]
+  uint32_t bar_off;   // full[4], empty[4], acc_full[2], acc_empty[2], rec_full[8], rec_empty[8];
                       // tensor-memory base, abort flag
   uint32_t stg_off;   // [128][kT2StgStride] accumulator rows staged for the reductions
   uint32_t total;
@@ -77,10 +78,8 @@ __host__ __device__ constexpr T2Layout t2_layout() {
   T2Layout L{};
   L.b_off = 0;
   L.rec_off = kT2Stages * 2u * kT2BBytes;
-  L.tab_off = L.rec_off + kTcRing * kT2SlotBytes;
-  L.tab_bytes = 2u * kTcK * kT2Pad * 4u + kTcK * 8u + kTcK * 8u;
-  L.bar_off = (L.tab_off + 2u * L.tab_bytes + 15u) & ~15u;
-  L.stg_off = L.bar_off + 16u * 8u + 16u;
+  L.bar_off = (L.rec_off + kT2Ring * kT2SlotBytes + 15u) & ~15u;
+  L.stg_off = L.bar_off + (12u + 2u * kT2Ring) * 8u + 16u;
   L.total = L.stg_off + 128u * kT2StgStride * 4u;
   return L;
 }
@@ -99,27 +98,27 @@ __global__ void __launch_bounds__(kT2Threads, 1) k_spread2_tm(const float2* __re
   uint64_t* empty = full + 4;                                       // [4] MMAs of stage s complete
   uint64_t* acc_full = full + 8;                                    // [2] accumulator set s complete
   uint64_t* acc_empty = full + 10;                                  // [2] accumulator set s read out
-  uint64_t* tab_full = full + 12;                                   // [2] table buffer b written
-  uint64_t* tab_empty = full + 14;                                  // [2] table buffer b read
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + L.bar_off + 128);
-  volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + L.bar_off + 132);
+  uint64_t* rec_full = full + 12;                                   // [kT2Ring] records of slot r landed
+  uint64_t* rec_empty = rec_full + kT2Ring;                         // [kT2Ring] slot r read
+  unsigned char* const bar_end = smem + L.bar_off + (12u + 2u * kT2Ring) * 8u;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar_end);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(bar_end + 4);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int num_items = *bins.num_items;
   const int G = (int)gridDim.x;
 
-  // the tap tables are zero outside the taps, which the table warps rewrite per batch
-  for (int i = tid; i < (int)(2u * L.tab_bytes / 4u); i += kT2Threads)
-    reinterpret_cast<float*>(smem + L.tab_off)[i] = 0.f;
   if (tid == 0) {
     for (int i = 0; i < 4; ++i) {
-      tc::mbar_init(&full[i], kT2AWarps + kT2BWarps);  // one arrival per operand warp
+      tc::mbar_init(&full[i], kT2OpWarps);  // one arrival per operand warp of the batch's set
       tc::mbar_init(&empty[i], 1);
     }
     for (int i = 0; i < 2; ++i) {
       tc::mbar_init(&acc_full[i], 1);
-      tc::mbar_init(&acc_empty[i], 4);                 // one arrival per epilogue warp
-      tc::mbar_init(&tab_full[i], 2);                  // one arrival per table warp
-      tc::mbar_init(&tab_empty[i], kT2AWarps + kT2BWarps);
+      tc::mbar_init(&acc_empty[i], 4);      // one arrival per epilogue warp
+    }
+    for (int i = 0; i < kT2Ring; ++i) {
+      tc::mbar_init(&rec_full[i], 1);       // the record warp
+      tc::mbar_init(&rec_empty[i], kT2OpWarps);
     }
     *abort_flag = 0;
     tc::mbar_fence_init();
@@ -134,148 +133,108 @@ __global__ void __launch_bounds__(kT2Threads, 1) k_spread2_tm(const float2* __re
   const uint32_t tmem = *tmem_slot;
   bool healthy = true;
 
-  auto tab_w = [&](uint32_t b, int dim) {
-    return reinterpret_cast<float*>(smem + L.tab_off + b * L.tab_bytes) + dim * kTcK * kT2Pad;
-  };
-  auto tab_val = [&](uint32_t b) {
-    return reinterpret_cast<float2*>(smem + L.tab_off + b * L.tab_bytes + 2u * kTcK * kT2Pad * 4u);
-  };
-  auto tab_off = [&](uint32_t b) {
-    return reinterpret_cast<int2*>(smem + L.tab_off + b * L.tab_bytes + 2u * kTcK * kT2Pad * 4u + kTcK * 8u);
-  };
-
   // Every role walks items c, c + G, ... (CTA c) in batches of kTcK nodes; batch gb
-  // (counted across the CTA's items) uses operand stage gb % 4 in its cycle gb / 4, table
-  // buffer gb & 1 and record slot gb % kTcRing; item k of the CTA accumulates into set k & 1.
-  if (warp >= kT2TabWarp0 && warp < kT2MmaWarp) {
-    // ======================= table warps =======================
-    const int half = warp - kT2TabWarp0;
+  // (counted across the CTA's items) uses operand stage gb % 4 in its cycle gb / 4, record
+  // slot gb % kT2Ring and operand set gb % 2; item k of the CTA accumulates into set k % 2.
+  if (warp == kT2RecWarp) {
+    // ======================= record warp =======================
     const float* sfrac = reinterpret_cast<const float*>(bins.sfrac);
     const float2* fperm = reinterpret_cast<const float2*>(bins.fperm);
-    const float norm = (float)geo.norm;
-    const float bscale = norm * tc_scale_b(bins, norm);
-    const float mf = (float)geo.m;
-    const int j = lane & (kTcK - 1), dim = lane >> 4;
-    const TapK kd = tap_k<WIN>(geo, dim);
-    const float sc = dim == 0 ? kTcScaleA : 1.f;  // A = w0 2^10
-    constexpr int kHalf = W / 2;
-    // the records of one batch into ring slot `slot` (warp kT2TabWarp0 only)
-    auto load = [&](const TcCursor& c, int slot) {
-      unsigned char* sl = smem + L.rec_off + slot * kT2SlotBytes;
-      const int base = c.item.y + c.b * kTcK, n = min(kTcK, c.item.z - base);
+    TcCursor lc;
+    tc_cursor_init(lc, bins, num_items);
+    uint32_t gb = 0;
+    for (; lc.it < num_items; tc_cursor_step(lc, bins, num_items), ++gb) {
+      const uint32_t r = gb % kT2Ring;
+      // slot r free once both operand sets' warps of batch gb - kT2Ring have read it
+      if (gb >= (uint32_t)kT2Ring &&
+          !tc::mbar_wait_warp(&rec_empty[r], ((gb / kT2Ring) - 1u) & 1u, kTcPolls)) {
+        healthy = false;
+        break;
+      }
+      if (*abort_flag != 0) {
+        healthy = false;
+        break;
+      }
+      unsigned char* sl = smem + L.rec_off + r * kT2SlotBytes;
+      const int base = lc.item.y + lc.b * kTcK, n = min(kTcK, lc.item.z - base);
       if (lane < kTcK) {
         if (lane < n) {
           cp_async4(sl + kT2SlotOff + lane * 4, bins.soff + base + lane);
           cp_async8(sl + kT2SlotVal + lane * 8, fperm + base + lane);
         } else {
-          reinterpret_cast<int*>(sl + kT2SlotOff)[lane] = -1;  // no node: zero taps, zero sample
+          reinterpret_cast<uint32_t*>(sl + kT2SlotOff)[lane] = 0xffffffffu;  // no node: zero taps
           reinterpret_cast<float2*>(sl + kT2SlotVal)[lane] = make_float2(0.f, 0.f);
         }
       }
       if (lane < 2 * n) cp_async4(sl + kT2SlotFrac + lane * 4, sfrac + (int64_t)base * 2 + lane);
       else reinterpret_cast<float*>(sl + kT2SlotFrac)[lane] = 0.f;
-    };
-    TcCursor cc, lc;
-    tc_cursor_init(cc, bins, num_items);
-    lc = cc;
-    if (half == 0) {
-#pragma unroll
-      for (int d = 0; d < kTcAhead; ++d) {
-        if (lc.it < num_items) {
-          load(lc, d);
-          tc_cursor_step(lc, bins, num_items);
-        }
-        cp_async_commit();
+      cp_async_commit();
+      if (gb >= (uint32_t)kT2Ahead) {  // the records of batch gb - kT2Ahead have landed
+        cp_async_wait_group<kT2Ahead>();
+        tc::mbar_arrive_warp(&rec_full[(gb - kT2Ahead) % kT2Ring]);
       }
     }
-    uint32_t gb = 0;
-    for (; cc.it < num_items; tc_cursor_step(cc, bins, num_items), ++gb) {
-      const uint32_t tb = gb & 1u;
-      bool fail = false;
-      if (half == 0) cp_async_wait_group<kTcAhead - 1>();  // the records of batch gb have landed
-      // table buffer tb free once the operand warps have read batch gb - 2 from it
-      if (gb >= 2 && lane == 0)
-        fail = !tc::mbar_wait_bounded(&tab_empty[tb], ((gb - 2u) >> 1) & 1u, kTcPolls);
-      if (tc::named_sync_or(3, 64, fail || *abort_flag != 0)) {  // records visible to both table warps
-        healthy = false;
-        break;
-      }
-      const unsigned char* sl = smem + L.rec_off + (gb % kTcRing) * kT2SlotBytes;
-      const uint32_t off = reinterpret_cast<const uint32_t*>(sl + kT2SlotOff)[j];
-      const bool node = off != 0xffffffffu;
-      // taps of half `half` of the window: l = half kHalf .. (half + 1) kHalf - 1
-      {
-        const float fr = reinterpret_cast<const float*>(sl + kT2SlotFrac)[j * 2 + dim];
-        float* const row = tab_w(tb, dim) + j * kT2Pad + kT2Zero;
-#pragma unroll
-        for (int i = 0; i < kHalf; ++i) {
-          const int l = half * kHalf + i;
-          row[l] = node ? tc_tap<WIN>(fr, mf, l, W, kd) * sc : 0.f;
-        }
-      }
-      if (half == 0 && lane < kTcK) {
-        const float2 v = reinterpret_cast<const float2*>(sl + kT2SlotVal)[j];
-        tab_val(tb)[j] = make_float2(v.x * bscale, v.y * bscale);
-        // window starts inside the tile by construction; clamped so that table reads
-        // always stay inside the padded rows
-        const int o0 = node ? min((int)(off & MASK), kT2Zero - 1) : 0;
-        const int o1 = node ? min((int)((off >> SH) & MASK), kT2Zero - 1) : 0;
-        tab_off(tb)[j] = make_int2(o0, o1);
-      }
-      // the next record load into the slot batch gb - 1 used (both table warps are past it)
-      if (half == 0) {
-        if (lc.it < num_items) {
-          load(lc, (int)((gb + kTcAhead) % kTcRing));
-          tc_cursor_step(lc, bins, num_items);
-        }
-        cp_async_commit();
-      }
-      tc::mbar_arrive_warp(&tab_full[tb]);
-    }
-    if (half == 0) cp_async_wait_group<0>();
+    cp_async_wait_group<0>();
+    for (uint32_t b = gb > (uint32_t)kT2Ahead ? gb - kT2Ahead : 0u; b < gb; ++b)
+      tc::mbar_arrive_warp(&rec_full[b % kT2Ring]);
     if (!healthy) *abort_flag = 1;
-  } else if (warp < kT2AWarps + kT2BWarps) {
-    // ======================= operand warps: A (0-3) and B (4-8) =======================
-    const bool is_a = warp < kT2AWarps;
-    const int p0 = 32 * warp + lane;                      // A: row (TMEM lane)
-    const int bt = 32 * (warp - kT2AWarps) + lane;       // B: task
+  } else if (warp < kT2OpWarps || warp >= kT2OpSet1) {
+    // ======================= operand warps: A (0-3, 16-19) and B (4-8, 20-24) =======================
+    const uint32_t set = warp >= kT2OpSet1 ? 1u : 0u;
+    const int lw = warp - (set ? kT2OpSet1 : 0);
+    const bool is_a = lw < kT2AWarps;
+    const int p0 = 32 * lw + lane;                        // A: row (TMEM lane; warp % 4 == lw)
+    const int bt = 32 * (lw - kT2AWarps) + lane;         // B: task
     const int p1 = bt >> 1, h = bt & 1;
-    uint32_t gb = 0, st = 0, cyc = 0;
+    const float mf = (float)geo.m;
+    const TapK k0 = tap_k<WIN>(geo, 0), k1 = tap_k<WIN>(geo, 1);
+    const float norm = (float)geo.norm;
+    const float bscale = norm * tc_scale_b(bins, norm);
+    uint32_t gb = 0;
     TcCursor cc;
     tc_cursor_init(cc, bins, num_items);
     for (; cc.it < num_items; tc_cursor_step(cc, bins, num_items), ++gb) {
-      const uint32_t tb = gb & 1u;
-      bool ok = tc::mbar_wait_warp(&tab_full[tb], (gb >> 1) & 1u, kTcPolls);
-      if (ok && cyc > 0) ok = tc::mbar_wait_warp(&empty[st], (cyc - 1u) & 1u, kTcPolls);
+      if ((gb & 1u) != set) continue;
+      const uint32_t r = gb % kT2Ring, st = gb & 3u, cyc = gb >> 2;
+      bool ok = tc::mbar_wait_warp(&rec_full[r], (gb / kT2Ring) & 1u, kTcPolls, kT2Spin);
+      if (ok && cyc > 0) ok = tc::mbar_wait_warp(&empty[st], (cyc - 1u) & 1u, kTcPolls, kT2Spin);
       if (!ok || *abort_flag != 0) {
         healthy = false;
         break;
       }
-      const int2* offs = tab_off(tb);
+      const unsigned char* sl = smem + L.rec_off + r * kT2SlotBytes;
+      const uint32_t* offs = reinterpret_cast<const uint32_t*>(sl + kT2SlotOff);
+      const float2* frs = reinterpret_cast<const float2*>(sl + kT2SlotFrac);
       if (is_a) {
         tc::fence_after_sync();
-        const float* w0 = tab_w(tb, 0) + kT2Zero + p0;
         uint32_t hi[8], lo[8];
 #pragma unroll
         for (int c = 0; c < 8; ++c) {
-          const float2 v =
-              make_float2(w0[(2 * c) * kT2Pad - offs[2 * c].x], w0[(2 * c + 1) * kT2Pad - offs[2 * c + 1].x]);
-          tc_split2_f16(v, hi[c], lo[c]);
+          float v[2];
+#pragma unroll
+          for (int u = 0; u < 2; ++u) {
+            const int j = 2 * c + u;
+            const uint32_t off = offs[j];
+            const int l = p0 - (int)(off & MASK);  // no node: l < 0, a zero tap
+            v[u] = tc_tap<WIN>(frs[j].x, mf, l, W, k0) * kTcScaleA;
+          }
+          tc_split2_f16(make_float2(v[0], v[1]), hi[c], lo[c]);
         }
-        const uint32_t ta = tmem + ((uint32_t)(32 * warp) << 16) + kT2ACol0 + st * 16u;
+        const uint32_t ta = tmem + ((uint32_t)(32 * lw) << 16) + kT2ACol0 + st * 16u;
         tc::tmem_st8(ta, hi);
         tc::tmem_st8(ta + 8u, lo);
         tc::tmem_st_wait();
         tc::fence_before_sync();
       } else {
-        const float* w1 = tab_w(tb, 1) + kT2Zero + p1;
-        const float2* val = tab_val(tb);
+        const float2* val = reinterpret_cast<const float2*>(sl + kT2SlotVal);
         float re[8], im[8];
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
-          const int jj = 8 * h + u;
-          const float w = w1[jj * kT2Pad - offs[jj].y];
-          const float2 v = val[jj];
+          const int j = 8 * h + u;
+          const uint32_t off = offs[j];
+          const int l = off == 0xffffffffu ? -1 : p1 - (int)((off >> SH) & MASK);
+          const float w = tc_tap<WIN>(frs[j].y, mf, l, W, k1) * bscale;
+          const float2 v = val[j];
           re[u] = w * v.x;
           im[u] = w * v.y;
         }
@@ -292,11 +251,7 @@ __global__ void __launch_bounds__(kT2Threads, 1) k_spread2_tm(const float2* __re
         tc::fence_proxy_async_smem();  // generic-proxy operand writes -> tensor core
       }
       tc::mbar_arrive_warp(&full[st]);
-      tc::mbar_arrive_warp(&tab_empty[tb]);
-      if (++st == kT2Stages) {
-        st = 0;
-        ++cyc;
-      }
+      tc::mbar_arrive_warp(&rec_empty[r]);
     }
     if (!healthy) *abort_flag = 1;
   } else if (warp == kT2MmaWarp) {
@@ -320,7 +275,7 @@ __global__ void __launch_bounds__(kT2Threads, 1) k_spread2_tm(const float2* __re
         const uint32_t d = tmem + set * kT2N;
         const int nbatch = (item.z - item.y + kTcK - 1) / kTcK;
         for (int b = 0; b < nbatch && healthy; ++b, ++gb) {
-          healthy = tc::mbar_wait_bounded(&full[st], cyc & 1u, kTcPolls);
+          healthy = tc::mbar_wait_spin(&full[st], cyc & 1u, kTcPolls, kT2Spin);
           if (!healthy) break;
           tc::fence_after_sync();
           const uint64_t so = (uint64_t)st * d_stage;
@@ -344,7 +299,7 @@ __global__ void __launch_bounds__(kT2Threads, 1) k_spread2_tm(const float2* __re
       }
     }
     __syncwarp();
-  } else {
+  } else if (warp >= kT2EpiWarp0 && warp < kT2EpiWarp0 + 4) {
     // ======================= epilogue warps =======================
     // Per work item: thread (lane quarter q, lane) reads TMEM row p0 = 32 q + lane of the
     // item's accumulator set into its own staging row, releases the set, and adds the row

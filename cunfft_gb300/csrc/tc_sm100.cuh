@@ -91,10 +91,27 @@ __device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t* bar, uint32_t pari
 // Bounded wait for the phase with the given parity to complete.  Returns false
 // after max_polls unsuccessful polls, each of which suspends the thread for at
 // most 1 microsecond.
+__device__ __forceinline__ bool mbar_test_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.b32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint32_t max_polls) {
   for (uint32_t i = 0; i < max_polls; ++i)
     if (mbar_try_wait_sleep(bar, parity, 1000u)) return true;
   return false;
+}
+// The same, after first spinning on the non-blocking test for `spin` polls: a phase that
+// completes within a few hundred cycles is seen at once instead of after the suspended
+// thread wakes up.  For latency-bound hand-offs where the waiting warp has nothing else to do.
+__device__ __forceinline__ bool mbar_wait_spin(uint64_t* bar, uint32_t parity, uint32_t max_polls, uint32_t spin) {
+  for (uint32_t i = 0; i < spin; ++i)
+    if (mbar_test_wait(bar, parity)) return true;
+  return mbar_wait_bounded(bar, parity, max_polls);
 }
 
 // arrive (release) on the mbarrier once
@@ -142,9 +159,10 @@ __device__ __forceinline__ void mbar_arrive_warp(uint64_t* bar) {
   __syncwarp();
   if ((threadIdx.x & 31) == 0) mbar_arrive(bar);
 }
-__device__ __forceinline__ bool mbar_wait_warp(uint64_t* bar, uint32_t parity, uint32_t max_polls) {
+__device__ __forceinline__ bool mbar_wait_warp(uint64_t* bar, uint32_t parity, uint32_t max_polls,
+                                               uint32_t spin = 0) {
   uint32_t ok = 1;
-  if ((threadIdx.x & 31) == 0) ok = mbar_wait_bounded(bar, parity, max_polls) ? 1u : 0u;
+  if ((threadIdx.x & 31) == 0) ok = mbar_wait_spin(bar, parity, max_polls, spin) ? 1u : 0u;
   ok = __shfl_sync(0xffffffffu, ok, 0);
   __syncwarp();
   return ok != 0;

@@ -52,16 +52,15 @@ int main() {
   }
   {
     const T2Layout L = t2_layout();
-    CHECK(L.total <= kMaxSmem, "spread2: shared %u", L.total);
-    CHECK(L.rec_off % 16 == 0 && L.tab_off % 16 == 0 && L.tab_bytes % 16 == 0 && L.bar_off % 16 == 0 &&
-              L.stg_off % 16 == 0 && (kT2StgStride * 4) % 16 == 0,
+    CHECK(L.total <= kMaxSmem && L.total > 228u * 1024u / 2u, "spread2: shared %u (one CTA per SM)", L.total);
+    CHECK(L.rec_off % 16 == 0 && L.bar_off % 16 == 0 && L.stg_off % 16 == 0 && (kT2StgStride * 4) % 16 == 0 &&
+              kT2SlotBytes % 16 == 0 && kT2SlotVal % 8 == 0,
           "spread2: align");
     CHECK(kT2ACol0 + kT2Stages * 16u <= 512u, "spread2: tmem");
-    for (int W = 4; W <= 16; W += 2) {
+    CHECK(kT2Ahead < kT2Ring && kT2OpSet1 % 4 == 0 && kT2EpiWarp0 % 4 == 0 && kT2MmaWarp < kT2EpiWarp0,
+          "spread2: roles");
+    for (int W = 4; W <= 16; W += 2)
       CHECK(2 * (64 + W - 1) <= kT2N && kT2MaxT0 + W - 1 <= 128, "spread2 W %d: extents", W);
-      // table reads: row p0 < 128 or column p1 < 80 of a node with window start 0 <= o < 64
-      CHECK(kT2Zero + 127 <= kT2Pad - 1 && kT2Zero - 63 >= 0 && kT2Zero + W <= kT2Pad, "spread2 W %d: table rows", W);
-    }
   }
   std::printf("layout check: %d failures\n", fails);
   return fails == 0 ? 0 : 1;
