@@ -1,5 +1,6 @@
 // grid_interp_tc.cu -- launcher of the tensor-core 3D FP32 interpolation: the split of
-// the grid into padded, per-plane scaled FP16 hi/lo planes, then the TMA-fed kernel.
+// the grid into padded, per-plane scaled FP16 hi/lo planes (one kernel, one pass), then
+// the TMA-fed kernel.
 #include <cudaTypedefs.h>
 
 #include <algorithm>
@@ -30,10 +31,8 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_tiled() {
 void interp_tc_release(Plan& p) {
   cudaFree(p.it_split);
   cudaFree(p.it_pinv);
-  cudaFree(p.it_pmax);
   p.it_split = nullptr;
   p.it_pinv = nullptr;
-  p.it_pmax = nullptr;
   p.it_ready = false;
 }
 
@@ -52,7 +51,6 @@ cudaError_t interp_tc_prepare(Plan& p) {
   if (!p.it_split) {
     cudaError_t e = plan_malloc(&p.it_split, bytes);
     if (e == cudaSuccess) e = plan_malloc(&p.it_pinv, sizeof(float) * (size_t)(sd.P0 * p.geo.batch));
-    if (e == cudaSuccess) e = plan_malloc(&p.it_pmax, sizeof(uint32_t) * (size_t)(p.geo.n[0] * p.geo.batch));
     if (e != cudaSuccess) {
       interp_tc_release(p);
       return e;
@@ -77,16 +75,12 @@ template <int W>
 static cudaError_t launch_it(const Plan& p, const void* in, void* out, cudaStream_t st) {
   if (!interp_tc_supported(p) || !p.it_ready) return cudaErrorInvalidConfiguration;
   const ItSplit sd = it_split_dims(p.geo);
-  cudaError_t e = cudaMemsetAsync(p.it_pmax, 0, sizeof(uint32_t) * (size_t)(p.geo.n[0] * p.geo.batch), st);
+  // one CTA per SM at a time over the padded planes: the planes being split stay in L2
+  // between their two reads
+  const int sblocks = (int)std::min<int64_t>(sd.P0 * p.geo.batch, (int64_t)p.num_sms);
+  k_split_planes<<<sblocks, kItSplitThreads, 0, st>>>((const float2*)in, (__half*)p.it_split, p.it_pinv, p.geo, sd);
+  cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  const int64_t per_plane = p.geo.n[1] * p.geo.n[2] / 4;
-  const unsigned ysplit = (unsigned)std::max<int64_t>(1, std::min<int64_t>((per_plane + 255) / 256,
-                                                                          (int64_t)p.num_sms * 8 / p.geo.n[0] + 1));
-  k_plane_absmax<<<dim3((unsigned)(p.geo.n[0] * p.geo.batch), ysplit), 256, 0, st>>>((const float2*)in, p.it_pmax,
-                                                                                    p.geo);
-  const int64_t quads = sd.P0 * sd.P1 * (sd.P2s / 4) * p.geo.batch;
-  const int sblocks = (int)std::min<int64_t>((quads + 255) / 256, (int64_t)p.num_sms * 16);
-  k_split_pad<<<sblocks, 256, 0, st>>>((const float2*)in, p.it_pmax, (__half*)p.it_split, p.it_pinv, p.geo, sd);
   // 512 tensor-memory columns per CTA: at most one CTA per SM (more than half the
   // SM's 228 KB of shared memory), so tcgen05.alloc never waits
   const ItLayout L = it_layout();

@@ -20,7 +20,7 @@
 // padded plane p0 of the grid by 2^(14 - e_p0), 2^e_p0 >= its largest |Re|, |Im|;
 // the node threads fold the inverse plane scales into their w0 weights.
 //
-// The grid is first split (k_plane_absmax, k_split_pad) into those FP16 hi + lo parts of its real and
+// The grid is first split (k_split_planes) into those FP16 hi + lo parts of its real and
 // imaginary parts, each an array over the periodically padded index range
 // [0, n_t + W - 1) per dimension.  Every tile's padded box then lies inside the
 // arrays (no wrap), and one thread loads each chunk with four TMA boxes (hi re, hi im,
@@ -135,58 +135,62 @@ __device__ __forceinline__ void ld_quad(const float2* src, bool al16, float4& a,
   }
 }
 
-// Largest |Re|, |Im| of every grid plane (instance, i0 < n0) into pmax (float bits,
-// zeroed before the launch): blockIdx.y runs over the plane's quads, blockIdx.x over
-// the planes; one atomic per warp.
-__global__ void k_plane_absmax(const float2* __restrict__ g, uint32_t* __restrict__ pmax, Geom geo) {
-  const int64_t plane = blockIdx.x, per = geo.n[1] * geo.n[2] / 4;
-  const float2* src = g + plane * geo.n[1] * geo.n[2];
-  const bool al16 = (reinterpret_cast<uintptr_t>(g) & 15u) == 0;  // n1 n2 is a multiple of 8
-  float mx = 0.f;
-  for (int64_t e = blockIdx.y * (int64_t)blockDim.x + threadIdx.x; e < per; e += (int64_t)gridDim.y * blockDim.x) {
-    float4 a, b;
-    ld_quad(src + 4 * e, al16, a, b);
-    mx = fmaxf(mx, fmaxf(fmaxf(fmaxf(fabsf(a.x), fabsf(a.y)), fmaxf(fabsf(a.z), fabsf(a.w))),
-                         fmaxf(fmaxf(fabsf(b.x), fabsf(b.y)), fmaxf(fabsf(b.z), fabsf(b.w)))));
-  }
-  const uint32_t m = __reduce_max_sync(0xffffffffu, __float_as_uint(mx));
-  if ((threadIdx.x & 31) == 0 && m != 0u) atomicMax(pmax + plane, m);
-}
-
 // 2^(14 - e) with 2^e > mx, as the exponent e
-__device__ __forceinline__ int it_plane_exp(uint32_t mx_bits) {
+__device__ __forceinline__ int it_plane_exp(float mx) {
   int ex = 0;
-  frexpf(__uint_as_float(mx_bits), &ex);
+  frexpf(mx, &ex);
   return ex;
 }
 
-// One thread per 4 consecutive p2 of one padded row, a quad that never straddles the
-// grid's wrap (n2 % 8 == 0): FP16 hi + lo parts of the real and imaginary parts
-// scaled by the plane's 2^(14 - e); the thread of a plane's first quad also writes the
-// plane's inverse scale.
-__global__ void k_split_pad(const float2* __restrict__ g, const uint32_t* __restrict__ pmax, __half* __restrict__ out,
-                            float* __restrict__ inv_scale, Geom geo, ItSplit sd) {
-  const int64_t q4 = sd.P2s / 4, row_q = sd.P1 * q4, per = sd.P0 * row_q, total = per * geo.batch;
-  const int64_t comp = sd.P0 * sd.P1 * sd.P2s;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t inst = e / per, r = e - inst * per;
-    const int64_t i0 = r / row_q, r2 = r - i0 * row_q;
-    const int64_t i1 = r2 / q4, i2 = (r2 - i1 * q4) * 4;
-    const int64_t gp = inst * geo.n[0] + wrap_up(i0, geo.n[0]);  // grid plane
-    const int ex = it_plane_exp(pmax[gp]);
+constexpr int kItSplitThreads = 1024;
+
+// The grid's padded FP16 hi/lo planes in one pass over the grid.  CTA c takes padded
+// planes (instance, i0) c, c + G, ...: it reads grid plane i0 mod n0 once for its largest
+// |Re|, |Im| (a block reduction), then again (from L2: the CTAs' planes in flight stay well
+// below its size) to write the plane's P1 x P2s quads of FP16 hi + lo parts of the real
+// and imaginary parts, scaled by the plane's 2^(14 - e), and the plane's inverse scale.
+// A quad (4 consecutive p2 of one padded row) never straddles the grid's wrap (n2 % 8 == 0).
+__global__ void __launch_bounds__(kItSplitThreads) k_split_planes(const float2* __restrict__ g,
+                                                                   __half* __restrict__ out,
+                                                                   float* __restrict__ inv_scale, Geom geo,
+                                                                   ItSplit sd) {
+  __shared__ uint32_t wmax[kItSplitThreads / 32];
+  const int64_t plane_elems = geo.n[1] * geo.n[2], q4 = sd.P2s / 4, comp = sd.P0 * sd.P1 * sd.P2s;
+  const bool al16 = (reinterpret_cast<uintptr_t>(g) & 15u) == 0;  // n1 n2 is a multiple of 8
+  for (int64_t pl = blockIdx.x; pl < sd.P0 * geo.batch; pl += gridDim.x) {
+    const int64_t inst = pl / sd.P0, i0 = pl - inst * sd.P0;
+    const float2* src = g + (inst * geo.n[0] + wrap_up(i0, geo.n[0])) * plane_elems;
+    float mx = 0.f;
+    for (int64_t e = threadIdx.x; e < plane_elems / 4; e += blockDim.x) {
+      float4 a, b;
+      ld_quad(src + 4 * e, al16, a, b);
+      mx = fmaxf(mx, fmaxf(fmaxf(fmaxf(fabsf(a.x), fabsf(a.y)), fmaxf(fabsf(a.z), fabsf(a.w))),
+                           fmaxf(fmaxf(fabsf(b.x), fabsf(b.y)), fmaxf(fabsf(b.z), fabsf(b.w)))));
+    }
+    const uint32_t wm = __reduce_max_sync(0xffffffffu, __float_as_uint(mx));
+    if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = wm;
+    __syncthreads();
+    uint32_t m = 0;
+#pragma unroll 8
+    for (int w = 0; w < kItSplitThreads / 32; ++w) m = max(m, wmax[w]);
+    __syncthreads();  // wmax is rewritten by the next plane
+    const int ex = it_plane_exp(__uint_as_float(m));
     const float scale = ldexpf(1.f, kItLogB - ex);
-    if (r2 == 0) inv_scale[inst * sd.P0 + i0] = ldexpf(1.f, ex - kItLogB);
-    const float2* src = g + gp * geo.n[1] * geo.n[2] + wrap_up(i1, geo.n[1]) * geo.n[2] + wrap_up(i2, geo.n[2]);
-    float4 a, b;
-    ld_quad(src, (reinterpret_cast<uintptr_t>(g) & 15u) == 0, a, b);
-    __half* o = out + inst * 4 * comp + (i0 * sd.P1 + i1) * sd.P2s + i2;
-    uint2 h, l;
-    it_split4_f16(make_float4(a.x * scale, a.z * scale, b.x * scale, b.z * scale), h, l);
-    *reinterpret_cast<uint2*>(o) = h;
-    *reinterpret_cast<uint2*>(o + 2 * comp) = l;
-    it_split4_f16(make_float4(a.y * scale, a.w * scale, b.y * scale, b.w * scale), h, l);
-    *reinterpret_cast<uint2*>(o + comp) = h;
-    *reinterpret_cast<uint2*>(o + 3 * comp) = l;
+    if (threadIdx.x == 0) inv_scale[inst * sd.P0 + i0] = ldexpf(1.f, ex - kItLogB);
+    __half* const o_plane = out + inst * 4 * comp + i0 * sd.P1 * sd.P2s;
+    for (int64_t e = threadIdx.x; e < sd.P1 * q4; e += blockDim.x) {
+      const int64_t i1 = e / q4, i2 = (e - i1 * q4) * 4;
+      float4 a, b;
+      ld_quad(src + wrap_up(i1, geo.n[1]) * geo.n[2] + wrap_up(i2, geo.n[2]), al16, a, b);
+      __half* o = o_plane + i1 * sd.P2s + i2;
+      uint2 h, l;
+      it_split4_f16(make_float4(a.x * scale, a.z * scale, b.x * scale, b.z * scale), h, l);
+      *reinterpret_cast<uint2*>(o) = h;
+      *reinterpret_cast<uint2*>(o + 2 * comp) = l;
+      it_split4_f16(make_float4(a.y * scale, a.w * scale, b.y * scale, b.w * scale), h, l);
+      *reinterpret_cast<uint2*>(o + comp) = h;
+      *reinterpret_cast<uint2*>(o + 3 * comp) = l;
+    }
   }
 }
 

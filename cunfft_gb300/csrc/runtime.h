@@ -67,7 +67,6 @@ struct Plan {
   // inverse scales and their TMA map, created before its first launch (interp_tc_prepare)
   void* it_split = nullptr;
   float* it_pinv = nullptr;
-  uint32_t* it_pmax = nullptr;
   CUtensorMap it_tmap{};
   bool it_ready = false;
 };
