@@ -56,12 +56,48 @@ def parse_args():
     # tips the choice, so the default run skips the autotuner and profiles the same kernels.
     ap.add_argument("--autotune", action="store_true", help="run the autotuner before the timed steps")
     ap.add_argument("--no-autotune", action="store_true", help="(default) keep the plan's default tiling")
-    ap.add_argument("--case", choices=["interp", "spread", "step"],
-                    help="profiling case: bind nodes once, then launch only this stage (3 times)")
+    ap.add_argument("--case", choices=["interp", "spread", "step", "spread2d", "interp2d"],
+                    help="profiling case: bind nodes once, then launch only this stage (3 times); the 2D cases "
+                         "run the batched 2D workload (64 x N=256^2, m=5, log-uniform M)")
     ap.add_argument("--precision", default="f32", choices=["f32", "f64"])
     ap.add_argument("--M", type=int, default=M_FULL)
     ap.add_argument("--tile", default="", help="tile extents for --case, e.g. 8,4,16")
     return ap.parse_args()
+
+
+def run_case2d(args):
+    """Three launches of 2D spreading or interpolation on the batched 2D workload."""
+    import numpy as np
+    import torch
+
+    from cunfft_gb300.nfft import NFFT
+
+    dev = torch.device("cuda", 0)
+    rng = np.random.default_rng(404)
+    B, N, m = 64, [256, 256], 5
+    Ms = np.round(10 ** rng.uniform(3, 6, B)).astype(np.int64)
+    Mt = int(Ms.sum())
+    x = torch.from_numpy(rng.uniform(-0.5, 0.5, (Mt, 2))).to(dev)
+    f = _crand_t(Mt, rng, dev, torch.complex64)
+    p = NFFT(N, m=m, precision="f32", batch=B, device=dev).set_nodes(x, Ms.tolist())
+    grid = p.grid()
+    out = torch.empty(Mt, dtype=torch.complex64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    times = []
+    for _ in range(3):
+        if args.case == "spread2d":
+            grid.zero_()
+        a.record(stream)
+        if args.case == "spread2d":
+            p.spread(f, grid)
+        else:
+            p.interp(grid, out=out)
+        b.record(stream)
+        b.synchronize()
+        times.append(a.elapsed_time(b))
+    print(json.dumps({"case": args.case, "M": Mt, "tiling": p.tiling(), "ms": times}))
+    p.close()
 
 
 def run_case(args):
@@ -69,6 +105,9 @@ def run_case(args):
     import torch
 
     from cunfft_gb300.nfft import NFFT
+
+    if args.case in ("spread2d", "interp2d"):
+        return run_case2d(args)
 
     dev = torch.device("cuda", 0)
     g = torch.Generator(device=dev).manual_seed(20240)

@@ -3,7 +3,7 @@
 //
 // The reference's adjoint gridding (kernelConvWithGauss_adjoint_*, src/cunfft_kernel.cu:
 // 608-1197), with the same window-start rule and taps, as the same product as k_spread_tc
-// (kernels_spread_tc.cuh): per batch of kTcK = 16 nodes of a tile, D += A B^T with
+// (kernels_spread_tc.cuh): per batch of kTmK = 32 nodes of a tile, D += A B^T with
 //     A[(p0, p1), j]     = w0_j[p0 - o0_j] w1_j[p1 - o1_j]      (FP16 hi + lo, x 2^10)
 //     B[(p2, re|im), j]  = w2_j[p2 - o2_j] (Re f_j | Im f_j)    (FP16 hi + lo, x 2^(14 - e))
 // and the three products hi*hi + hi*lo + lo*hi accumulated in FP32.  Here the builder
@@ -16,8 +16,9 @@
 // row (p0, p1) with p0 = a + AP mt; lanes with a >= AP or p0 >= E0 hold zero rows of
 // A.  The thread owning lane L keeps its w1 row in registers over its M-tiles.
 // Tensor memory (512 columns): the work item's accumulators in columns [0, 256)
-// (M-tile mt at 64 mt, column 2 p2 + re|im) and kTmStages A stages in [256, 512)
-// (stage s, M-tile mt: hi in 256 + 64 s + 16 mt .. + 7, lo in the next 8 columns).
+// (M-tile mt at 64 mt, column 2 p2 + re|im) and kTmStages = 2 A stages in [256, 512)
+// (stage s, M-tile mt: hi in 256 + 128 s + 32 mt .. + 15, lo in the next 16 columns; each
+// batch is two MMA k-steps of 16 nodes, columns 8 ks of each part).
 // There is one accumulator set: the MMAs of a work item's first batch wait, M-tile by
 // M-tile, until the epilogue has read that M-tile of the previous item out.
 //
@@ -45,11 +46,18 @@ constexpr int kTmBWarps = kTmBuilders - kTmAWarps;  // 20 warps in all: 96 regis
 constexpr int kTmMmaWarp = kTmBuilders;         // lane 0 issues the MMAs
 constexpr int kTmEpiWarp0 = kTmBuilders + 1;    // 4 epilogue warps: lane quarter warp % 4
 constexpr int kTmThreads = (kTmBuilders + 1 + 4) * 32;
-constexpr int kTmStages = 4;                    // operand stages (A in TMEM, B in shared memory)
+constexpr int kTmK = 32;                        // nodes per batch: two FP16 MMA k-steps of 16
+constexpr int kTmStages = 2;                    // operand stages (A in TMEM, B in shared memory)
 constexpr int kTmMaxMt = 4;                     // M-tiles: 4 x 64 accumulator columns
 constexpr uint32_t kTmACol0 = 256;              // first A-stage column
-constexpr uint32_t kTmAStageCols = 64;          // 4 M-tiles x (8 hi + 8 lo) columns
-constexpr uint32_t kTmBStage = 2u * kTcN * kTcK * 2u;  // B hi + B lo of one stage
+constexpr uint32_t kTmAStageCols = 128;         // 4 M-tiles x (16 hi + 16 lo) columns
+constexpr uint32_t kTmBPart = kTcN * kTmK * 2u; // B hi (or lo) of one stage
+constexpr uint32_t kTmBStage = 2u * kTmBPart;
+constexpr uint32_t kTmSBO = (kTmK / 8) * 128u;  // B: 8-row groups of kTmK / 8 core matrices
+constexpr int kTmWxStride = 36;                 // floats per weight-table row: 8 consecutive rows, distinct banks
+constexpr int kTmWbStride = 40;                 // floats per B-table row: rows two apart 16 banks apart
+constexpr int kTmRing = 4;                      // record slots, loaded kTmRing - 1 batches ahead
+constexpr uint32_t kTmSlotOff = 0, kTmSlotFrac = kTmK * 4, kTmSlotVal = kTmK * 16, kTmSlotBytes = kTmK * 24;
 constexpr int kTmStgStride = kTcN + 4;          // floats per staging row: 8 consecutive rows, distinct banks
 
 __host__ __device__ constexpr int tm_e1(int W) { return fixed_t_mid(3, W) + W - 1; }
@@ -64,10 +72,10 @@ __host__ __device__ constexpr bool spread_tm_ok(int d, int W, int T0, int E0) {
 // Shared-memory layout of k_spread_tm (byte offsets; host and device agree).
 struct TmLayout {
   int mt;               // M-tiles covering the tile's E0 planes
-  uint32_t rec_off;     // kTcRing record slots (B stages at offset 0)
-  uint32_t wx_off;      // 2 x ([E0][kTcWxStride] w0 over planes, [E1][kTcWxStride] w1 over rows)
+  uint32_t rec_off;     // kTmRing record slots (B stages at offset 0)
+  uint32_t wx_off;      // 2 x ([E0][kTmWxStride] w0 over planes, [E1][kTmWxStride] w1 over rows)
   uint32_t wx_stage;
-  uint32_t wb_off;      // 2 x [kTcN][kTcWbStride] B values w2 f (rows 2 p2 + re|im, 16 nodes)
+  uint32_t wb_off;      // 2 x [kTcN][kTmWbStride] B values w2 f (rows 2 p2 + re|im, kTmK nodes)
   uint32_t wb_stage;
   uint32_t bar_off;     // full[4], empty[4], acc_full[4], acc_empty[4]; tensor-memory base
   uint32_t stg_off;     // [4 x 128][kTmStgStride] accumulator rows staged for the atomics
@@ -78,14 +86,24 @@ __host__ __device__ inline TmLayout tm_layout(int W, int E0) {
   TmLayout L{};
   L.mt = tm_mt(W, E0);
   L.rec_off = kTmStages * kTmBStage;
-  L.wx_off = L.rec_off + kTcRing * kTcSlotBytes;
-  L.wx_stage = (uint32_t)(E0 + tm_e1(W)) * kTcWxStride * 4u;
+  L.wx_off = L.rec_off + kTmRing * kTmSlotBytes;
+  L.wx_stage = (uint32_t)(E0 + tm_e1(W)) * kTmWxStride * 4u;
   L.wb_off = (L.wx_off + 2u * L.wx_stage + 15u) & ~15u;
-  L.wb_stage = (uint32_t)kTcN * kTcWbStride * 4u;
+  L.wb_stage = (uint32_t)kTcN * kTmWbStride * 4u;
   L.bar_off = L.wb_off + 2u * L.wb_stage;
   L.stg_off = L.bar_off + 16u * 8u + 16u;
   L.total = L.stg_off + (uint32_t)kTmMaxMt * 128u * kTmStgStride * 4u;
   return L;
+}
+
+// TcCursor step over batches of kTmK nodes
+__device__ __forceinline__ void tm_cursor_step(TcCursor& c, const Bins& bins, int num_items) {
+  const int G = (int)gridDim.x;
+  if (c.item.y + (++c.b) * kTmK < c.item.z) return;
+  c.it += G;
+  c.b = 0;
+  c.item = c.next;
+  c.next = c.it + G < num_items ? bins.items[c.it + G] : make_int4(0, 0, 0, 0);
 }
 
 template <int W, int WIN>
@@ -96,7 +114,7 @@ __global__ void __launch_bounds__(kTmThreads, 1) k_spread_tm(const float2* __res
   constexpr uint32_t MASK = (1u << SH) - 1u;
   constexpr int kBuildThreads = kTmBuilders * 32;
   static_assert(2 * (fixed_t_last(3, W) + W - 1) <= kTcN, "complex columns must fit the MMA N");
-  static_assert(kTcK == 16 && kTcN == 64, "staging roles assume 16 nodes and 64 B rows");
+  static_assert(kTmK == 32 && kTcN == 64, "staging roles assume 32 nodes and 64 B rows");
   static_assert(AP >= 1, "a plane's rows must fit one M-tile");
   extern __shared__ __align__(16) unsigned char smem[];
   const int E0 = tl.E[0];
@@ -148,42 +166,42 @@ __global__ void __launch_bounds__(kTmThreads, 1) k_spread_tm(const float2* __res
     const int aq = warp & 3, amt = (warp >> 2) & 1, aL = 32 * aq + lane;
     const int aa = aL / E1, ap1 = aL - aa * E1;
     const bool a_row = aa < AP;
-    // loads of one batch's records into ring slot `slot` (threads < 4 kTcK)
+    // loads of one batch's records into ring slot `slot` (threads < 4 kTmK)
     auto load = [&](const TcCursor& c, int slot) {
-      unsigned char* sl = smem + L.rec_off + slot * kTcSlotBytes;
-      const int base = c.item.y + c.b * kTcK, n = min(kTcK, c.item.z - base);
-      if (tid < kTcK) {
+      unsigned char* sl = smem + L.rec_off + slot * kTmSlotBytes;
+      const int base = c.item.y + c.b * kTmK, n = min(kTmK, c.item.z - base);
+      if (tid < kTmK) {
         if (tid < n) {
-          cp_async4(sl + kTcSlotOff + tid * 4, bins.soff + base + tid);
-          cp_async8(sl + kTcSlotVal + tid * 8, fperm + base + tid);
+          cp_async4(sl + kTmSlotOff + tid * 4, bins.soff + base + tid);
+          cp_async8(sl + kTmSlotVal + tid * 8, fperm + base + tid);
         } else {
-          reinterpret_cast<int*>(sl + kTcSlotOff)[tid] = -1;
-          reinterpret_cast<float2*>(sl + kTcSlotVal)[tid] = make_float2(0.f, 0.f);
+          reinterpret_cast<int*>(sl + kTmSlotOff)[tid] = -1;
+          reinterpret_cast<float2*>(sl + kTmSlotVal)[tid] = make_float2(0.f, 0.f);
         }
-      } else if (tid < 4 * kTcK) {
-        const int i = tid - kTcK;
-        if (i < 3 * n) cp_async4(sl + kTcSlotFrac + i * 4, sfrac + (int64_t)base * 3 + i);
-        else reinterpret_cast<float*>(sl + kTcSlotFrac)[i] = 0.f;
+      } else if (tid < 4 * kTmK) {
+        const int i = tid - kTmK;
+        if (i < 3 * n) cp_async4(sl + kTmSlotFrac + i * 4, sfrac + (int64_t)base * 3 + i);
+        else reinterpret_cast<float*>(sl + kTmSlotFrac)[i] = 0.f;
       }
     };
     TcCursor cc, lc;  // the batch being built and the batch being loaded
     tc_cursor_init(cc, bins, num_items);
     lc = cc;
 #pragma unroll
-    for (int d = 0; d < kTcAhead; ++d) {
+    for (int d = 0; d < kTmRing - 1; ++d) {
       if (lc.it < num_items) {
         load(lc, d);
-        tc_cursor_step(lc, bins, num_items);
+        tm_cursor_step(lc, bins, num_items);
       }
       cp_async_commit();
     }
-    cp_async_wait_group<kTcAhead - 1>();
+    cp_async_wait_group<kTmRing - 2>();
     tc::named_sync(1, kBuildThreads);  // records of batch 0 visible
     uint32_t gb = 0, st = 0, cyc = 0;
-    for (; cc.it < num_items; tc_cursor_step(cc, bins, num_items), ++gb) {
+    for (; cc.it < num_items; tm_cursor_step(cc, bins, num_items), ++gb) {
       if (lc.it < num_items) {
-        load(lc, (int)((gb + kTcAhead) % kTcRing));
-        tc_cursor_step(lc, bins, num_items);
+        load(lc, (int)((gb + kTmRing - 1) % kTmRing));
+        tm_cursor_step(lc, bins, num_items);
       }
       cp_async_commit();
       // stage st (its B buffer and its A columns) is free once the MMAs of batch gb - 4
@@ -191,10 +209,10 @@ __global__ void __launch_bounds__(kTmThreads, 1) k_spread_tm(const float2* __res
       bool fail = false;
       if (cyc > 0 && tid == kBuildThreads - 32) fail = !tc::mbar_wait_bounded(&empty[st], (cyc - 1u) & 1u, kTcPolls);
       healthy &= !fail;
-      const unsigned char* sl = smem + L.rec_off + (gb % kTcRing) * kTcSlotBytes;
-      const uint32_t* roff = reinterpret_cast<const uint32_t*>(sl + kTcSlotOff);
-      const float* frac = reinterpret_cast<const float*>(sl + kTcSlotFrac);
-      const float2* val = reinterpret_cast<const float2*>(sl + kTcSlotVal);
+      const unsigned char* sl = smem + L.rec_off + (gb % kTmRing) * kTmSlotBytes;
+      const uint32_t* roff = reinterpret_cast<const uint32_t*>(sl + kTmSlotOff);
+      const float* frac = reinterpret_cast<const float*>(sl + kTmSlotFrac);
+      const float2* val = reinterpret_cast<const float2*>(sl + kTmSlotVal);
       float* wx = reinterpret_cast<float*>(smem + L.wx_off + (size_t)(gb & 1u) * L.wx_stage);
       float* wb = reinterpret_cast<float*>(smem + L.wb_off + (size_t)(gb & 1u) * L.wb_stage);
       if (warp >= kTmAWarps) {
@@ -203,31 +221,35 @@ __global__ void __launch_bounds__(kTmThreads, 1) k_spread_tm(const float2* __res
         // planes (dd = 0) or rows (dd = 1) w, w + kTmBWarps, ...; lane (node j, half h)
         // the B values w2 f of columns p2 = 2 w + h + 2 kTmBWarps i < 32 (p2 >= E2 gives
         // zero taps)
-        const int bw = warp - kTmAWarps, j = lane & (kTcK - 1), hd = lane >> 4;
-        const uint32_t off = roff[j];
-        {
-          const float fr = frac[j * 3 + hd];
-          const int o = hd ? (int)((off >> SH) & MASK) : (int)(off & MASK);
-          const int Ed = hd ? E1 : E0;
-          const TapK kd = hd ? k1 : k0;
-          const float sc = hd ? kTcScaleA : 1.f;  // w1 carries the A scale 2^10
-          float* const col = wx + (hd ? E0 : 0) * kTcWxStride + j;
-          for (int p = bw; p < Ed; p += kTmBWarps) col[p * kTcWxStride] = tc_tap<WIN>(fr, mf, p - o, W, kd) * sc;
-        }
-        const int o2 = (int)(off >> (2 * SH));
-        const float fr2 = frac[j * 3 + 2];
-        const float2 c = val[j];
-        float* const col = wb + j;
+        const int bw = warp - kTmAWarps, hd = lane >> 4;
 #pragma unroll
-        for (int i = 0; i < (kTcN / 2 + 2 * kTmBWarps - 1) / (2 * kTmBWarps); ++i) {
-          const int p2 = 2 * bw + hd + 2 * kTmBWarps * i;
-          if (p2 >= kTcN / 2) break;
-          const float w2 = tc_tap<WIN>(fr2, mf, p2 - o2, W, k2) * bscale;
-          col[(2 * p2) * kTcWbStride] = w2 * c.x;
-          col[(2 * p2 + 1) * kTcWbStride] = w2 * c.y;
+        for (int jh = 0; jh < kTmK / 16; ++jh) {  // the batch's node halves
+          const int j = 16 * jh + (lane & 15);
+          const uint32_t off = roff[j];
+          {
+            const float fr = frac[j * 3 + hd];
+            const int o = hd ? (int)((off >> SH) & MASK) : (int)(off & MASK);
+            const int Ed = hd ? E1 : E0;
+            const TapK kd = hd ? k1 : k0;
+            const float sc = hd ? kTcScaleA : 1.f;  // w1 carries the A scale 2^10
+            float* const col = wx + (hd ? E0 : 0) * kTmWxStride + j;
+            for (int p = bw; p < Ed; p += kTmBWarps) col[p * kTmWxStride] = tc_tap<WIN>(fr, mf, p - o, W, kd) * sc;
+          }
+          const int o2 = (int)(off >> (2 * SH));
+          const float fr2 = frac[j * 3 + 2];
+          const float2 c = val[j];
+          float* const col = wb + j;
+#pragma unroll
+          for (int i = 0; i < (kTcN / 2 + 2 * kTmBWarps - 1) / (2 * kTmBWarps); ++i) {
+            const int p2 = 2 * bw + hd + 2 * kTmBWarps * i;
+            if (p2 >= kTcN / 2) break;
+            const float w2 = tc_tap<WIN>(fr2, mf, p2 - o2, W, k2) * bscale;
+            col[(2 * p2) * kTmWbStride] = w2 * c.x;
+            col[(2 * p2 + 1) * kTmWbStride] = w2 * c.y;
+          }
         }
       }
-      cp_async_wait_group<kTcAhead - 1>();  // this thread's loads of batch gb + 1 have landed
+      cp_async_wait_group<kTmRing - 2>();  // this thread's loads of batch gb + 1 have landed
       // (1) done; stage st free, tables and next records visible; the builders leave
       // together when any of them saw a wait give up or the abort flag raised
       if (tc::named_sync_or(1, kBuildThreads, fail || *abort_flag != 0)) {
@@ -237,55 +259,63 @@ __global__ void __launch_bounds__(kTmThreads, 1) k_spread_tm(const float2* __res
       if (warp < kTmAWarps) {
         // (2) A rows of lane aL, M-tiles amt and amt + 2: w0 (w1 2^10) -> FP16 hi, lo
         tc::fence_after_sync();
-        float2 w1r[kTcK / 2];
-        if (a_row) {
-#pragma unroll
-          for (int c4 = 0; c4 < kTcK / 4; ++c4) {
-            const float4 t = *reinterpret_cast<const float4*>(wx + (E0 + ap1) * kTcWxStride + 4 * c4);
-            w1r[2 * c4] = make_float2(t.x, t.y);
-            w1r[2 * c4 + 1] = make_float2(t.z, t.w);
-          }
-        } else {
-#pragma unroll
-          for (int k = 0; k < kTcK / 2; ++k) w1r[k] = make_float2(0.f, 0.f);
-        }
         const uint32_t tq = tmem + ((uint32_t)(32 * aq) << 16) + kTmACol0 + st * kTmAStageCols;
 #pragma unroll
-        for (int i = 0; i < 2; ++i) {
-          const int mt = amt + 2 * i;
-          if (mt < L.mt) {
-            const int p0 = aa + AP * mt;
-            uint32_t hi[8], lo[8];
-            if (a_row && p0 < E0) {
+        for (int kh = 0; kh < kTmK / 16; ++kh) {  // nodes 16 kh .. 16 kh + 15: columns 8 kh of each part
+          float2 w1r[8];
+          if (a_row) {
 #pragma unroll
-              for (int c4 = 0; c4 < kTcK / 4; ++c4) {
-                const float4 t = *reinterpret_cast<const float4*>(wx + p0 * kTcWxStride + 4 * c4);
-                tc_split2_f16(__fmul2_rn(make_float2(t.x, t.y), w1r[2 * c4]), hi[2 * c4], lo[2 * c4]);
-                tc_split2_f16(__fmul2_rn(make_float2(t.z, t.w), w1r[2 * c4 + 1]), hi[2 * c4 + 1], lo[2 * c4 + 1]);
-              }
-            } else {
-#pragma unroll
-              for (int c = 0; c < 8; ++c) hi[c] = lo[c] = 0u;
+            for (int c4 = 0; c4 < 4; ++c4) {
+              const float4 t = *reinterpret_cast<const float4*>(wx + (E0 + ap1) * kTmWxStride + 16 * kh + 4 * c4);
+              w1r[2 * c4] = make_float2(t.x, t.y);
+              w1r[2 * c4 + 1] = make_float2(t.z, t.w);
             }
-            tc::tmem_st8(tq + (uint32_t)(16 * mt), hi);
-            tc::tmem_st8(tq + (uint32_t)(16 * mt + 8), lo);
+          } else {
+#pragma unroll
+            for (int k = 0; k < 8; ++k) w1r[k] = make_float2(0.f, 0.f);
+          }
+#pragma unroll
+          for (int i = 0; i < 2; ++i) {
+            const int mt = amt + 2 * i;
+            if (mt < L.mt) {
+              const int p0 = aa + AP * mt;
+              uint32_t hi[8], lo[8];
+              if (a_row && p0 < E0) {
+#pragma unroll
+                for (int c4 = 0; c4 < 4; ++c4) {
+                  const float4 t = *reinterpret_cast<const float4*>(wx + p0 * kTmWxStride + 16 * kh + 4 * c4);
+                  tc_split2_f16(__fmul2_rn(make_float2(t.x, t.y), w1r[2 * c4]), hi[2 * c4], lo[2 * c4]);
+                  tc_split2_f16(__fmul2_rn(make_float2(t.z, t.w), w1r[2 * c4 + 1]), hi[2 * c4 + 1], lo[2 * c4 + 1]);
+                }
+              } else {
+#pragma unroll
+                for (int c = 0; c < 8; ++c) hi[c] = lo[c] = 0u;
+              }
+              tc::tmem_st8(tq + (uint32_t)(32 * mt + 8 * kh), hi);
+              tc::tmem_st8(tq + (uint32_t)(32 * mt + 16 + 8 * kh), lo);
+            }
           }
         }
         tc::tmem_st_wait();
         tc::fence_before_sync();
       } else {
         // (2) B rows 8 rg + ri (lane ri = lane & 7) of row groups rg = w, w + kTmBWarps < 8,
-        // nodes 4 q4 .. 4 q4 + 3 -> FP16 hi, lo
+        // nodes 4 q .. 4 q + 3 (q = q4, q4 + 4) -> FP16 hi, lo
         const int ri = lane & 7, q4 = lane >> 3;
         unsigned char* b_hi = smem + (size_t)st * kTmBStage;
         for (int rg = warp - kTmAWarps; rg < kTcN / 8; rg += kTmBWarps) {
-          const float4 t = *reinterpret_cast<const float4*>(wb + (rg * 8 + ri) * kTcWbStride + 4 * q4);
-          const float vv[4] = {t.x, t.y, t.z, t.w};
-          uint2 hi, lo;
-          tc_split4_f16(vv, hi, lo);
-          const uint32_t o = tc_elem_off(rg, ri, q4 >> 1) + (uint32_t)(q4 & 1) * 8u;
-          *reinterpret_cast<uint2*>(b_hi + o) = hi;
-          *reinterpret_cast<uint2*>(b_hi + kTcN * kTcK * 2 + o) = lo;
+#pragma unroll
+          for (int kh = 0; kh < kTmK / 16; ++kh) {
+            const int q = q4 + 4 * kh;
+            const float4 t = *reinterpret_cast<const float4*>(wb + (rg * 8 + ri) * kTmWbStride + 4 * q);
+            const float vv[4] = {t.x, t.y, t.z, t.w};
+            uint2 hi, lo;
+            tc_split4_f16(vv, hi, lo);
+            const uint32_t o = (uint32_t)rg * kTmSBO + (uint32_t)(q >> 1) * kTcLBO + (uint32_t)ri * 16u +
+                               (uint32_t)(q & 1) * 8u;
+            *reinterpret_cast<uint2*>(b_hi + o) = hi;
+            *reinterpret_cast<uint2*>(b_hi + kTmBPart + o) = lo;
+          }
         }
         tc::fence_proxy_async_smem();  // generic-proxy operand writes -> tensor core
       }
@@ -300,8 +330,8 @@ __global__ void __launch_bounds__(kTmThreads, 1) k_spread_tm(const float2* __res
     // ======================= MMA issuer: lane 0 =======================
     if (lane == 0) {
       const uint32_t sb0 = tc::smem_u32(smem);
-      const uint64_t d_bh = tc::smem_desc(sb0, kTcLBO, kTcSBO);
-      const uint64_t d_bl = tc::smem_desc(sb0 + kTcN * kTcK * 2, kTcLBO, kTcSBO);
+      const uint64_t d_bh = tc::smem_desc(sb0, kTcLBO, kTmSBO);
+      const uint64_t d_bl = tc::smem_desc(sb0 + kTmBPart, kTcLBO, kTmSBO);
       const uint64_t d_stage = (uint64_t)(kTmBStage >> 4);  // stage s = stage 0 + s d_stage
       const uint32_t idesc = tc::idesc_f16(128, kTcN);
       uint32_t gb = 0, st = 0, cyc = 0, k = 0;
@@ -309,7 +339,7 @@ __global__ void __launch_bounds__(kTmThreads, 1) k_spread_tm(const float2* __res
       for (int it = blockIdx.x; it < num_items; it += G, ++k) {
         const int4 item = nxt;
         if (it + G < num_items) nxt = bins.items[it + G];  // one item ahead
-        const int nbatch = (item.z - item.y + kTcK - 1) / kTcK;
+        const int nbatch = (item.z - item.y + kTmK - 1) / kTmK;
         for (int b = 0; b < nbatch && healthy; ++b, ++gb) {
           healthy = tc::mbar_wait_bounded(&full[st], cyc & 1u, kTcPolls);
           if (!healthy) break;
@@ -321,10 +351,15 @@ __global__ void __launch_bounds__(kTmThreads, 1) k_spread_tm(const float2* __res
               healthy &= tc::mbar_wait_bounded(&acc_empty[mt], (k - 1u) & 1u, kTcPolls);
               tc::fence_after_sync();
             }
-            const uint32_t d = tmem + (uint32_t)(mt * kTcN), am = ta + (uint32_t)(16 * mt);
-            tc::mma_f16_ta(d, am, d_bh + so, idesc, b > 0 ? 1u : 0u);  // K = 16: the whole batch
-            tc::mma_f16_ta(d, am, d_bl + so, idesc, 1u);
-            tc::mma_f16_ta(d, am + 8u, d_bh + so, idesc, 1u);
+            const uint32_t d = tmem + (uint32_t)(mt * kTcN), am = ta + (uint32_t)(32 * mt);
+#pragma unroll
+            for (int ks = 0; ks < kTmK / 16; ++ks) {  // k-steps of 16 nodes: A columns 8 ks, B 256 ks bytes
+              const uint64_t kb = (uint64_t)(ks * 2 * kTcLBO) >> 4;
+              const uint32_t ak = am + (uint32_t)(8 * ks);
+              tc::mma_f16_ta(d, ak, d_bh + so + kb, idesc, (b > 0 || ks > 0) ? 1u : 0u);
+              tc::mma_f16_ta(d, ak, d_bl + so + kb, idesc, 1u);
+              tc::mma_f16_ta(d, ak + 16u, d_bh + so + kb, idesc, 1u);
+            }
             if (b == nbatch - 1) tc::mma_commit(&acc_full[mt]);
           }
           tc::mma_commit(&empty[st]);
