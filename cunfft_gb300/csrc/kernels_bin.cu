@@ -57,7 +57,15 @@ __global__ void k_bin_count(const double* __restrict__ x, int64_t M, Geom geo, T
       tile = tile * tl.nb[t] + (s >> (__ffs(tl.T[t]) - 1));  // T_t is a power of two
     }
     tile += (int64_t)inst * tl.tiles_per_inst;
-    int rank = atomicAdd(&count[tile], 1);
+    // one atomic per tile and warp: the lanes that share a tile (clustered nodes fill a
+    // few tiles) take consecutive ranks from their leader's single add
+    const unsigned act = __activemask();
+    const unsigned peers = __match_any_sync(act, (unsigned long long)tile);
+    const int leader = __ffs(peers) - 1, lane = threadIdx.x & 31;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(&count[tile], __popc(peers));
+    base = __shfl_sync(act, base, leader);
+    const int rank = base + __popc(peers & ((1u << lane) - 1u));
     tile_rank[j] = make_int2((int)tile, rank);
   }
 }
