@@ -62,6 +62,9 @@ def parse_args():
     ap.add_argument("--precision", default="f32", choices=["f32", "f64"])
     ap.add_argument("--M", type=int, default=M_FULL)
     ap.add_argument("--tile", default="", help="tile extents for --case, e.g. 8,4,16")
+    ap.add_argument("--kernel", default="auto", choices=["auto", "shared", "register", "tensor"],
+                    help="gridding kernel form for --case (spreading: shared, register or tensor; "
+                         "interpolation: shared or tensor)")
     return ap.parse_args()
 
 
@@ -80,6 +83,8 @@ def run_case2d(args):
     x = torch.from_numpy(rng.uniform(-0.5, 0.5, (Mt, 2))).to(dev)
     f = _crand_t(Mt, rng, dev, torch.complex64)
     p = NFFT(N, m=m, precision="f32", batch=B, device=dev).set_nodes(x, Ms.tolist())
+    if args.kernel != "auto":
+        (p.set_spread_kernel if args.case == "spread2d" else p.set_interp_kernel)(args.kernel)
     grid = p.grid()
     out = torch.empty(Mt, dtype=torch.complex64, device=dev)
     stream = torch.cuda.current_stream(dev)
@@ -122,6 +127,11 @@ def run_case(args):
     if args.tile:
         p.set_tiling([int(v) for v in args.tile.split(",")])
     p.set_nodes(x)
+    if args.kernel != "auto":
+        if args.case in ("spread", "step"):
+            p.set_spread_kernel(args.kernel)
+        if args.case in ("interp", "step") and args.kernel != "register":
+            p.set_interp_kernel(args.kernel)
     grid = p.grid()
     out = torch.empty(M, dtype=cd, device=dev)
     stream = torch.cuda.current_stream(dev)

@@ -215,6 +215,9 @@ __global__ void __launch_bounds__(kTmThreads, 1) k_spread_tm(const float2* __res
       const float2* val = reinterpret_cast<const float2*>(sl + kTmSlotVal);
       float* wx = reinterpret_cast<float*>(smem + L.wx_off + (size_t)(gb & 1u) * L.wx_stage);
       float* wb = reinterpret_cast<float*>(smem + L.wb_off + (size_t)(gb & 1u) * L.wb_stage);
+      // a batch of at most 16 nodes (most of an item's last batch) needs only the first
+      // node half: its second k-step is neither built nor multiplied
+      const int halves = cc.item.z - (cc.item.y + cc.b * kTmK) > 16 ? 2 : 1;
       if (warp >= kTmAWarps) {
         // (1) the B warps evaluate every table of the batch (the A warps' phase (2) is
         // the long one): lane (node j, dimension dd) of warp kTmAWarps + w the taps of
@@ -224,6 +227,7 @@ __global__ void __launch_bounds__(kTmThreads, 1) k_spread_tm(const float2* __res
         const int bw = warp - kTmAWarps, hd = lane >> 4;
 #pragma unroll
         for (int jh = 0; jh < kTmK / 16; ++jh) {  // the batch's node halves
+          if (jh >= halves) break;
           const int j = 16 * jh + (lane & 15);
           const uint32_t off = roff[j];
           {
@@ -262,6 +266,7 @@ __global__ void __launch_bounds__(kTmThreads, 1) k_spread_tm(const float2* __res
         const uint32_t tq = tmem + ((uint32_t)(32 * aq) << 16) + kTmACol0 + st * kTmAStageCols;
 #pragma unroll
         for (int kh = 0; kh < kTmK / 16; ++kh) {  // nodes 16 kh .. 16 kh + 15: columns 8 kh of each part
+          if (kh >= halves) break;
           float2 w1r[8];
           if (a_row) {
 #pragma unroll
@@ -306,6 +311,7 @@ __global__ void __launch_bounds__(kTmThreads, 1) k_spread_tm(const float2* __res
         for (int rg = warp - kTmAWarps; rg < kTcN / 8; rg += kTmBWarps) {
 #pragma unroll
           for (int kh = 0; kh < kTmK / 16; ++kh) {
+            if (kh >= halves) break;
             const int q = q4 + 4 * kh;
             const float4 t = *reinterpret_cast<const float4*>(wb + (rg * 8 + ri) * kTmWbStride + 4 * q);
             const float vv[4] = {t.x, t.y, t.z, t.w};
@@ -341,6 +347,7 @@ __global__ void __launch_bounds__(kTmThreads, 1) k_spread_tm(const float2* __res
         if (it + G < num_items) nxt = bins.items[it + G];  // one item ahead
         const int nbatch = (item.z - item.y + kTmK - 1) / kTmK;
         for (int b = 0; b < nbatch && healthy; ++b, ++gb) {
+          const int halves = item.z - (item.y + b * kTmK) > 16 ? 2 : 1;  // k-steps built (as the builders)
           healthy = tc::mbar_wait_bounded(&full[st], cyc & 1u, kTcPolls);
           if (!healthy) break;
           tc::fence_after_sync();
@@ -354,6 +361,7 @@ __global__ void __launch_bounds__(kTmThreads, 1) k_spread_tm(const float2* __res
             const uint32_t d = tmem + (uint32_t)(mt * kTcN), am = ta + (uint32_t)(32 * mt);
 #pragma unroll
             for (int ks = 0; ks < kTmK / 16; ++ks) {  // k-steps of 16 nodes: A columns 8 ks, B 256 ks bytes
+              if (ks >= halves) break;
               const uint64_t kb = (uint64_t)(ks * 2 * kTcLBO) >> 4;
               const uint32_t ak = am + (uint32_t)(8 * ks);
               tc::mma_f16_ta(d, ak, d_bh + so + kb, idesc, (b > 0 || ks > 0) ? 1u : 0u);

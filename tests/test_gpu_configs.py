@@ -83,7 +83,9 @@ def test_config3_clustered_2d(dev):
     p32 = NFFT(N, m=6, precision="f32", device=dev).set_nodes(xt)
     f32 = p32.forward(torch.from_numpy(fh).to(dev))
     fh32 = p32.adjoint(torch.from_numpy(f).to(dev))
-    assert _rel(f64, f32) < 1e-5 and _rel(fh64, fh32) < 1e-5
+    # the FP32 form against the FP64 form on identical inputs: the FP32 gridding's own error
+    # (measured 3.6e-7 forward, 9.1e-7 adjoint), below the window's ~1e-6 against the NDFT
+    assert _rel(f64, f32) < 2e-6 and _rel(fh64, fh32) < 2e-6
     # FP64 NDFT on subsamples: 2048 nodes (forward), 2048 coefficients (adjoint)
     idx = torch.from_numpy(rng.choice(M, 2048, replace=False)).to(dev)
     sub = NFFT(N, m=6, device=dev).set_nodes(xt[idx].contiguous())
@@ -138,6 +140,10 @@ def test_config4_batched_uneven_graph(dev):
     nd_h = full.ndft_adjoint_at(f, kidx).reshape(B, -1)
     got_h = out_fh.reshape(B, -1)[:, kidx]
     assert _rel(nd_h, got_h) < 1e-5
+    # the FP32 replay against the FP64 form on the same instances (measured 2.8e-7 forward,
+    # 6.3e-7 adjoint)
+    assert _rel(full.forward(fh), out_f) < 2e-6
+    assert _rel(full.adjoint(f), out_fh) < 2e-6
     for q in (p, sub, full):
         q.close()
 
