@@ -106,9 +106,13 @@ __global__ void k_bin_scatter(const double* __restrict__ x, int64_t M, Geom geo,
 }
 
 // Single-CTA exclusive scan of the per-tile counts and of the per-tile work-item
-// counts ceil(count / chunk).  Each thread scans a contiguous segment (loads
-// unrolled so several are in flight); the segment totals are scanned with warp
-// shuffles and one shared-memory pass over the 32 warp totals.
+// counts ceil(count / chunk), in rounds of 1024 x kScanPer tiles: thread t takes tiles
+// kScanPer t .. kScanPer t + kScanPer - 1 of the round (the loads of a warp together
+// cover one contiguous kilobyte), the thread totals are scanned with warp
+// shuffles and one shared-memory pass over the 32 warp totals, and the round's total
+// carries into the next round.
+constexpr int kScanPer = 8;
+
 __device__ __forceinline__ void warp_incl_scan2(int64_t& a, int64_t& b) {
   const int lane = threadIdx.x & 31;
 #pragma unroll
@@ -125,44 +129,52 @@ __global__ void __launch_bounds__(1024) k_scan_tiles(const int32_t* __restrict__
                                                      int32_t* __restrict__ tile_off, int32_t* __restrict__ item_off,
                                                      int32_t* __restrict__ num_items) {
   __shared__ int64_t wc[32], wi[32];
-  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
-  const int64_t seg = (ntiles + nt - 1) / nt;
-  const int64_t lo = min(ntiles, tid * seg), hi = min(ntiles, lo + seg);
-  int64_t c = 0, it = 0;
-#pragma unroll 8
-  for (int64_t i = lo; i < hi; ++i) {
-    const int32_t v = count[i];
-    c += v;
-    it += (v + chunk - 1) / chunk;
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+  int64_t run_c = 0, run_i = 0;  // totals of the rounds before (the same in every thread)
+  for (int64_t r0 = 0; r0 < ntiles; r0 += (int64_t)nt * kScanPer) {
+    const int64_t lo = r0 + (int64_t)tid * kScanPer;
+    int32_t v[kScanPer], w[kScanPer];
+    int64_t c = 0, it = 0;
+#pragma unroll
+    for (int k = 0; k < kScanPer; ++k) {
+      v[k] = lo + k < ntiles ? count[lo + k] : 0;
+      w[k] = (v[k] + chunk - 1) / chunk;
+      c += v[k];
+      it += w[k];
+    }
+    int64_t ic = c, ii = it;  // inclusive scan over the block
+    warp_incl_scan2(ic, ii);
+    if (lane == 31) {
+      wc[warp] = ic;
+      wi[warp] = ii;
+    }
+    __syncthreads();
+    if (warp == 0) {
+      int64_t a = lane < nw ? wc[lane] : 0, b = lane < nw ? wi[lane] : 0;
+      warp_incl_scan2(a, b);
+      wc[lane] = a;
+      wi[lane] = b;
+    }
+    __syncthreads();
+    int64_t rc = run_c + (warp > 0 ? wc[warp - 1] : 0) + ic - c;
+    int64_t ri = run_i + (warp > 0 ? wi[warp - 1] : 0) + ii - it;
+#pragma unroll
+    for (int k = 0; k < kScanPer; ++k) {
+      if (lo + k < ntiles) {
+        tile_off[lo + k] = (int32_t)rc;
+        item_off[lo + k] = (int32_t)ri;
+      }
+      rc += v[k];
+      ri += w[k];
+    }
+    run_c += wc[nw - 1];
+    run_i += wi[nw - 1];
+    __syncthreads();  // wc / wi are rewritten by the next round
   }
-  int64_t ic = c, ii = it;  // inclusive scan over the block
-  warp_incl_scan2(ic, ii);
-  if (lane == 31) {
-    wc[warp] = ic;
-    wi[warp] = ii;
-  }
-  __syncthreads();
-  if (warp == 0) {
-    int64_t a = lane < nt / 32 ? wc[lane] : 0, b = lane < nt / 32 ? wi[lane] : 0;
-    warp_incl_scan2(a, b);
-    wc[lane] = a;
-    wi[lane] = b;
-  }
-  __syncthreads();
-  const int64_t base_c = warp > 0 ? wc[warp - 1] : 0, base_i = warp > 0 ? wi[warp - 1] : 0;
-  int64_t rc = base_c + ic - c, ri = base_i + ii - it;
-#pragma unroll 8
-  for (int64_t i = lo; i < hi; ++i) {
-    const int32_t v = count[i];
-    tile_off[i] = (int32_t)rc;
-    item_off[i] = (int32_t)ri;
-    rc += v;
-    ri += (v + chunk - 1) / chunk;
-  }
-  if (tid == nt - 1) {
-    tile_off[ntiles] = (int32_t)(base_c + ic);
-    item_off[ntiles] = (int32_t)(base_i + ii);
-    *num_items = (int32_t)(base_i + ii);
+  if (tid == 0) {
+    tile_off[ntiles] = (int32_t)run_c;
+    item_off[ntiles] = (int32_t)run_i;
+    *num_items = (int32_t)run_i;
   }
 }
 
