@@ -131,6 +131,14 @@ struct Tiling {
   int use_global;        // 1: no shared-memory tile fits, grid in global memory
   int spread_kernel;     // spreading kernel in use: CUNFFT_X_SPREAD_SHARED, _REGISTER, _TENSOR or _GLOBAL
   int interp_kernel;     // interpolation kernel in use: CUNFFT_X_INTERP_SHARED, _TENSOR or _GLOBAL
+  // Sub-bins (2D FP32 plans the tensor-core interpolation covers, sub_on = 1): the
+  // counting sort orders the nodes of a tile by sub-tile of 2^ssh[0] x 2^ssh[1] window
+  // starts, sub-bin (s0, s1) = s0 snb1 + s1 of ns per tile, and the binning also makes the
+  // sub-bins' interpolation items; sub_on = 0: tile order only (ns = 1)
+  int sub_on;
+  int ns;
+  int ssh[2];
+  int snb1;
 };
 
 // Sorted node records, produced by the binning kernels.
@@ -149,10 +157,20 @@ struct Bins {
   int32_t* inst_off;     // [batch + 1] node offsets per instance
   int32_t* status;       // [1] device-side error flag
   uint32_t* fmax;        // [1] largest |Re|, |Im| of the samples being spread (float bits), per call
+  // sub-bins (Tiling::sub_on): the counting sort's key is tile * ns + sub-bin
+  int32_t* scount;       // [tiles_total * ns + 1] nodes per sub-bin
+  int32_t* sub_off;      // [tiles_total * ns + 1] exclusive scan of scount: first sorted node of each sub-bin
+  int32_t* iitem_off;    // [tiles_total * ns + 1] exclusive scan of the sub-bins' interpolation items
+  int4*    iitems;       // [max_iitems] (sub-bin key, start, end, 0): at most kSubItem nodes of one sub-tile
+  int32_t* num_iitems;   // [1]
+  int64_t  max_iitems;
   int64_t  M;            // total nodes
   int64_t  max_items;
   int      valid;        // nodes binned for the current tiling
 };
+
+// nodes per interpolation item of a sub-bin (the MMA's M)
+constexpr int kSubItem = 128;
 
 // i mod n in [0, n) for any i: a mask when n is a power of two, else the remainder.
 __host__ __device__ inline int64_t wrap_n(int64_t i, int64_t n) {

@@ -1,6 +1,6 @@
-// grid_interp_tc.cu -- launcher of the tensor-core 3D FP32 interpolation: the split of
-// the grid into padded, per-plane scaled FP16 hi/lo planes (one kernel, one pass), then
-// the TMA-fed kernel.
+// grid_interp_tc.cu -- launcher of the tensor-core FP32 interpolation: the split of the
+// grid into padded, per-plane scaled FP16 hi/lo planes (one kernel, one pass), then the
+// TMA-fed kernel; the 2D form's rows and kernel are in grid_interp2_tc.cu.
 #include <cudaTypedefs.h>
 
 #include <algorithm>
@@ -9,7 +9,13 @@
 
 namespace cg {
 
+// the 2D form (grid_interp2_tc.cu)
+bool interp2_tc_supported(const Plan& p);
+cudaError_t interp2_tc_prepare(Plan& p, PFN_cuTensorMapEncodeTiled_v12000 enc);
+cudaError_t grid_launch_interp2_tc(const Plan& p, const void* in, void* out, cudaStream_t st);
+
 bool interp_tc_supported(const Plan& p) {
+  if (p.geo.d == 2) return interp2_tc_supported(p);
   return p.prec == kF32 && !p.tl.use_global && interp_tc_ok(p.geo.d, p.geo.W, p.tl.T[0], p.geo.n[2]);
 }
 
@@ -43,6 +49,7 @@ void interp_tc_release(Plan& p) {
 // bytes (P2s % 8 == 0).
 cudaError_t interp_tc_prepare(Plan& p) {
   if (p.it_ready) return cudaSuccess;
+  if (p.geo.d == 2) return interp2_tc_prepare(p, encode_tiled());
   const ItSplit sd = it_split_dims(p.geo);
   const size_t comp = (size_t)(sd.P0 * sd.P1 * sd.P2s);
   const size_t bytes = sizeof(__half) * 4 * comp * (size_t)p.geo.batch;
@@ -98,6 +105,7 @@ static cudaError_t launch_it(const Plan& p, const void* in, void* out, cudaStrea
 }
 
 cudaError_t grid_launch_interp_tc(const Plan& p, const void* in, void* out, cudaStream_t st) {
+  if (p.geo.d == 2) return grid_launch_interp2_tc(p, in, out, st);
   switch (p.geo.W) {
     case 4: return launch_it<4>(p, in, out, st);
     case 6: return launch_it<6>(p, in, out, st);

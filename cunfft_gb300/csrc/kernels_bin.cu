@@ -43,6 +43,7 @@ __global__ void k_bin_count(const double* __restrict__ x, int64_t M, Geom geo, T
   for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < M; j += (int64_t)gridDim.x * blockDim.x) {
     int inst = geo.batch > 1 ? find_instance(inst_off, geo.batch, j) : 0;
     int64_t tile = 0;
+    int sub = 0;  // sub-bin of the window start inside the tile (Tiling::sub_on)
     for (int t = 0; t < d; ++t) {
       const double xt = x[j * d + t];
       int64_t u;
@@ -55,8 +56,13 @@ __global__ void k_bin_count(const double* __restrict__ x, int64_t M, Geom geo, T
       }
       int64_t s = wrap_n(u, geo.n[t]);
       tile = tile * tl.nb[t] + (s >> (__ffs(tl.T[t]) - 1));  // T_t is a power of two
+      if (tl.sub_on && t < 2) {
+        const int o = (int)(s & (tl.T[t] - 1));
+        sub = t == 0 ? (o >> tl.ssh[0]) * tl.snb1 : sub + (o >> tl.ssh[1]);
+      }
     }
     tile += (int64_t)inst * tl.tiles_per_inst;
+    if (tl.sub_on) tile = tile * tl.ns + sub;  // the counting sort's key
     // one atomic per tile and warp: the lanes that share a tile (clustered nodes fill a
     // few tiles) take consecutive ranks from their leader's single add
     const unsigned act = __activemask();
@@ -106,12 +112,12 @@ __global__ void k_bin_scatter(const double* __restrict__ x, int64_t M, Geom geo,
 }
 
 // Single-CTA exclusive scan of the per-tile counts and of the per-tile work-item
-// counts ceil(count / chunk), in rounds of 1024 x kScanPer tiles: thread t takes tiles
-// kScanPer t .. kScanPer t + kScanPer - 1 of the round (the loads of a warp together
-// cover one contiguous kilobyte), the thread totals are scanned with warp
-// shuffles and one shared-memory pass over the 32 warp totals, and the round's total
-// carries into the next round.
-constexpr int kScanPer = 8;
+// counts ceil(count / chunk), in rounds of kScanRound tiles: warp w takes the 256
+// tiles w * 256 .. w * 256 + 255 of the round, lane l the tiles l, l + 32, ... of them,
+// so every load and store of a warp is one contiguous 128-byte line.  A warp scans its
+// tiles in eight steps of 32 (warp shuffles, carrying the step totals), the 32 warp
+// totals are scanned in shared memory, and the round's total carries into the next.
+constexpr int kScanRound = 1024 * 8;
 
 __device__ __forceinline__ void warp_incl_scan2(int64_t& a, int64_t& b) {
   const int lane = threadIdx.x & 31;
@@ -129,24 +135,27 @@ __global__ void __launch_bounds__(1024) k_scan_tiles(const int32_t* __restrict__
                                                      int32_t* __restrict__ tile_off, int32_t* __restrict__ item_off,
                                                      int32_t* __restrict__ num_items) {
   __shared__ int64_t wc[32], wi[32];
-  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+  const int per = kScanRound / (int)blockDim.x;  // tiles per lane and round (8 at 1024 threads)
   int64_t run_c = 0, run_i = 0;  // totals of the rounds before (the same in every thread)
-  for (int64_t r0 = 0; r0 < ntiles; r0 += (int64_t)nt * kScanPer) {
-    const int64_t lo = r0 + (int64_t)tid * kScanPer;
-    int32_t v[kScanPer], w[kScanPer];
-    int64_t c = 0, it = 0;
+  for (int64_t r0 = 0; r0 < ntiles; r0 += kScanRound) {
+    const int64_t wb = r0 + (int64_t)warp * 32 * per;
+    int64_t ec[8], ei[8], cc = 0, ci = 0;  // exclusive prefixes within the warp's tiles
 #pragma unroll
-    for (int k = 0; k < kScanPer; ++k) {
-      v[k] = lo + k < ntiles ? count[lo + k] : 0;
-      w[k] = (v[k] + chunk - 1) / chunk;
-      c += v[k];
-      it += w[k];
+    for (int k = 0; k < 8; ++k) {
+      const int64_t e = wb + 32 * k + lane;
+      const int32_t v = (k < per && e < ntiles) ? count[e] : 0;
+      int64_t a = v, b = (v + chunk - 1) / chunk;
+      const int64_t v64 = a, w64 = b;
+      warp_incl_scan2(a, b);
+      ec[k] = cc + a - v64;
+      ei[k] = ci + b - w64;
+      cc += __shfl_sync(0xffffffffu, a, 31);
+      ci += __shfl_sync(0xffffffffu, b, 31);
     }
-    int64_t ic = c, ii = it;  // inclusive scan over the block
-    warp_incl_scan2(ic, ii);
-    if (lane == 31) {
-      wc[warp] = ic;
-      wi[warp] = ii;
+    if (lane == 0) {
+      wc[warp] = cc;
+      wi[warp] = ci;
     }
     __syncthreads();
     if (warp == 0) {
@@ -156,16 +165,14 @@ __global__ void __launch_bounds__(1024) k_scan_tiles(const int32_t* __restrict__
       wi[lane] = b;
     }
     __syncthreads();
-    int64_t rc = run_c + (warp > 0 ? wc[warp - 1] : 0) + ic - c;
-    int64_t ri = run_i + (warp > 0 ? wi[warp - 1] : 0) + ii - it;
+    const int64_t bc = run_c + (warp > 0 ? wc[warp - 1] : 0), bi = run_i + (warp > 0 ? wi[warp - 1] : 0);
 #pragma unroll
-    for (int k = 0; k < kScanPer; ++k) {
-      if (lo + k < ntiles) {
-        tile_off[lo + k] = (int32_t)rc;
-        item_off[lo + k] = (int32_t)ri;
+    for (int k = 0; k < 8; ++k) {
+      const int64_t e = wb + 32 * k + lane;
+      if (k < per && e < ntiles) {
+        tile_off[e] = (int32_t)(bc + ec[k]);
+        item_off[e] = (int32_t)(bi + ei[k]);
       }
-      rc += v[k];
-      ri += w[k];
     }
     run_c += wc[nw - 1];
     run_i += wi[nw - 1];
@@ -176,6 +183,13 @@ __global__ void __launch_bounds__(1024) k_scan_tiles(const int32_t* __restrict__
     item_off[ntiles] = (int32_t)run_i;
     *num_items = (int32_t)run_i;
   }
+}
+
+// Nodes per tile from the sub-bin offsets (sub-bins of a tile are consecutive keys).
+__global__ void k_tile_counts(const int32_t* __restrict__ sub_off, int64_t ntiles, int ns,
+                              int32_t* __restrict__ count) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < ntiles; t += (int64_t)gridDim.x * blockDim.x)
+    count[t] = sub_off[(t + 1) * ns] - sub_off[t * ns];
 }
 
 __global__ void k_make_items(const int32_t* __restrict__ count, const int32_t* __restrict__ tile_off,
@@ -209,22 +223,37 @@ cudaError_t launch_binning(const Plan& p, const double* x, cudaStream_t st) {
       }
     lg.k[t] = k;
   }
-  cudaError_t e = cudaMemsetAsync(B.count, 0, sizeof(int32_t) * (tl.tiles_total + 1), st);
+  // counting sort over keys: tiles, or tile * ns + sub-bin with sub-bins; the positions
+  // come from the scan of the key counts, the tile-level items from the tile counts
+  const bool sub = tl.sub_on != 0;
+  const int64_t nkeys = tl.tiles_total * (sub ? tl.ns : 1);
+  int32_t* kcount = sub ? B.scount : B.count;
+  int32_t* koff = sub ? B.sub_off : B.tile_off;
+  cudaError_t e = cudaMemsetAsync(kcount, 0, sizeof(int32_t) * (nkeys + 1), st);
   if (e != cudaSuccess) return e;
   if (B.M > 0) {
-    k_bin_count<<<grid_for(B.M, 256, p.num_sms), 256, 0, st>>>(x, B.M, p.geo, tl, lg, B.inst_off, B.count,
+    k_bin_count<<<grid_for(B.M, 256, p.num_sms), 256, 0, st>>>(x, B.M, p.geo, tl, lg, B.inst_off, kcount,
                                                                  B.tile_rank);
+  }
+  if (sub) {
+    // sub-bin offsets and the interpolation items of at most kSubItem nodes per sub-bin
+    k_scan_tiles<<<1, 1024, 0, st>>>(B.scount, nkeys, kSubItem, B.sub_off, B.iitem_off, B.num_iitems);
+    k_tile_counts<<<grid_for(tl.tiles_total, 256, p.num_sms), 256, 0, st>>>(B.sub_off, tl.tiles_total, tl.ns,
+                                                                             B.count);
   }
   k_scan_tiles<<<1, 1024, 0, st>>>(B.count, tl.tiles_total, tl.chunk, B.tile_off, B.item_off, B.num_items);
   if (B.M > 0) {
     if (p.prec == kF64)
       k_bin_scatter<double><<<grid_for(B.M, 256, p.num_sms), 256, 0, st>>>(
-          x, B.M, p.geo, tl, lg, B.tile_rank, B.tile_off, B.sidx, B.soff, (double*)B.sfrac);
+          x, B.M, p.geo, tl, lg, B.tile_rank, koff, B.sidx, B.soff, (double*)B.sfrac);
     else
       k_bin_scatter<float><<<grid_for(B.M, 256, p.num_sms), 256, 0, st>>>(
-          x, B.M, p.geo, tl, lg, B.tile_rank, B.tile_off, B.sidx, B.soff, (float*)B.sfrac);
+          x, B.M, p.geo, tl, lg, B.tile_rank, koff, B.sidx, B.soff, (float*)B.sfrac);
     k_make_items<<<grid_for(tl.tiles_total, 256, p.num_sms), 256, 0, st>>>(B.count, B.tile_off, B.item_off,
                                                                             tl.tiles_total, tl.chunk, B.items);
+    if (sub)
+      k_make_items<<<grid_for(nkeys, 256, p.num_sms), 256, 0, st>>>(B.scount, B.sub_off, B.iitem_off, nkeys,
+                                                                      kSubItem, B.iitems);
   }
   return cudaGetLastError();
 }

@@ -150,7 +150,7 @@ constexpr int kItSplitThreads = 1024;
 // below its size) to write the plane's P1 x P2s quads of FP16 hi + lo parts of the real
 // and imaginary parts, scaled by the plane's 2^(14 - e), and the plane's inverse scale.
 // A quad (4 consecutive p2 of one padded row) never straddles the grid's wrap (n2 % 8 == 0).
-__global__ void __launch_bounds__(kItSplitThreads) k_split_planes(const float2* __restrict__ g,
+static __global__ void __launch_bounds__(kItSplitThreads) k_split_planes(const float2* __restrict__ g,
                                                                    __half* __restrict__ out,
                                                                    float* __restrict__ inv_scale, Geom geo,
                                                                    ItSplit sd) {

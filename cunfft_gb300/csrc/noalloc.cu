@@ -108,6 +108,8 @@ extern "C" int cunfft_x_spread_noalloc(int d, const int64_t* N, const int64_t* n
     fprintf(stderr, "cunfft_x_spread_noalloc: %s\n", p.last_msg);
     return s;
   }
+  p.tl.sub_on = 0;  // spreading needs the nodes in tile order only: no sub-bins, no room for them
+  p.tl.ns = 1;
   if (p.tl.tiles_total > kNaMaxTiles) {
     fprintf(stderr, "cunfft_x_spread_noalloc: the grid needs %lld tiles, beyond the fixed scratch limit of %lld\n",
             (long long)p.tl.tiles_total, (long long)kNaMaxTiles);

@@ -82,10 +82,17 @@ static void free_bins(Plan* p) {
   cudaFree(B.tile_off);
   cudaFree(B.item_off);
   cudaFree(B.items);
+  cudaFree(B.scount);
+  cudaFree(B.sub_off);
+  cudaFree(B.iitem_off);
+  cudaFree(B.iitems);
   B.sidx = nullptr; B.soff = nullptr; B.sfrac = nullptr; B.tile_rank = nullptr; B.fperm = nullptr;
   B.count = nullptr; B.tile_off = nullptr; B.item_off = nullptr; B.items = nullptr;
+  B.scount = nullptr; B.sub_off = nullptr; B.iitem_off = nullptr; B.iitems = nullptr;
+  B.max_iitems = 0;
   p->bins_capacity_M = -1;
   p->bins_capacity_tiles = -1;
+  p->bins_capacity_keys = -1;
 }
 
 // Default tile extents.  For d >= 2 only the outermost extent T0 is free: the
@@ -194,7 +201,9 @@ int plan_choose_tiling(Plan* p, const int* Tin, int chunk) {
     tl.threads = 128;
   }
   if (tl.tiles_total >= (int64_t)1 << 31) return set_status(p, CUNFFT_X_INVALID_ARGUMENT, "too many tiles");
+  interp2_tc_subbins(*p, tl);
   p->tl = tl;
+  p->it_ready = false;  // the interpolation's TMA boxes follow the tile extents: encoded again before use
   p->tl.spread_kernel = pick_spread_kernel(*p, p->spread_mode);
   p->tl.interp_kernel = pick_interp_kernel(*p, p->interp_mode);
   p->bins.valid = 0;
@@ -208,7 +217,8 @@ int plan_set_interp_kernel(Plan* p, int kind) {
     return set_status(p, CUNFFT_X_INVALID_ARGUMENT, "unknown interpolation kernel %d", kind);
   if (kind == CUNFFT_X_INTERP_TENSOR && !interp_tc_supported(*p))
     return set_status(p, CUNFFT_X_UNSUPPORTED,
-                      "tensor-core interpolation needs d = 3, FP32, 2m+2 <= 16, an outer tile extent <= 16 and n_3 >= 4");
+                      "tensor-core interpolation needs FP32 and 2m+2 <= 16, and in 3D an outer tile extent <= 16 "
+                      "and n_3 divisible by 8, in 2D an inner tile extent >= 16 and n_2 divisible by 8");
   p->interp_mode = kind;
   p->tl.interp_kernel = pick_interp_kernel(*p, kind);
   ++p->node_gen;
@@ -448,6 +458,7 @@ int plan_init(Plan* p, int d, const int64_t* N, const int64_t* n, int m, int pre
   CG_TRY(check_cuda(p, plan_malloc(&p->bins.inst_off, sizeof(int32_t) * (batch + 1)), "cudaMalloc"));
   CG_TRY(check_cuda(p, plan_malloc(&p->bins.work, sizeof(int32_t) * 2), "cudaMalloc"));
   CG_TRY(check_cuda(p, plan_malloc(&p->bins.num_items, sizeof(int32_t)), "cudaMalloc"));
+  CG_TRY(check_cuda(p, plan_malloc(&p->bins.num_iitems, sizeof(int32_t)), "cudaMalloc"));
   CG_TRY(check_cuda(p, plan_malloc(&p->bins.status, sizeof(int32_t)), "cudaMalloc"));
   CG_TRY(check_cuda(p, plan_malloc(&p->bins.fmax, sizeof(uint32_t)), "cudaMalloc"));
   CG_TRY(check_cuda(p, cudaMemset(p->bins.status, 0, sizeof(int32_t)), "cudaMemset"));
@@ -470,12 +481,14 @@ void plan_release(Plan* p) {
   cudaFree(p->bins.inst_off);
   cudaFree(p->bins.work);
   cudaFree(p->bins.num_items);
+  cudaFree(p->bins.num_iitems);
   cudaFree(p->bins.status);
   cudaFree(p->bins.fmax);
   p->bins.fmax = nullptr;
   p->bins.inst_off = nullptr;
   p->bins.work = nullptr;
   p->bins.num_items = nullptr;
+  p->bins.num_iitems = nullptr;
   p->bins.status = nullptr;
   if (p->own_g) cudaFree(p->g);
   p->g = nullptr;
@@ -495,9 +508,12 @@ static int ensure_bins(Plan* p, int64_t M) {
   Bins& B = p->bins;
   const int64_t tiles = p->tl.tiles_total;
   const int64_t max_items = tiles + M / std::max(1, p->tl.chunk) + 1;
+  // sub-bin keys and their interpolation items (each sub-bin: at most count / kSubItem + 1)
+  const int64_t keys = p->tl.sub_on ? tiles * p->tl.ns : 0;
+  const int64_t max_iitems = keys > 0 ? keys + M / kSubItem + 1 : 0;
   const size_t real = elem_bytes(p) / 2;
   if (M > p->bins_capacity_M || tiles > p->bins_capacity_tiles || max_items > B.max_items ||
-      p->bins_capacity_M < 0) {
+      keys > p->bins_capacity_keys || max_iitems > B.max_iitems || p->bins_capacity_M < 0) {
     const int64_t capM = std::max<int64_t>(M, 1), capT = tiles;
     free_bins(p);
     CG_TRY(check_cuda(p, plan_malloc(&B.sidx, sizeof(int32_t) * capM), "cudaMalloc bins"));
@@ -511,8 +527,17 @@ static int ensure_bins(Plan* p, int64_t M) {
     const int64_t cap_items = capT + capM / std::max(1, p->tl.chunk) + 1;
     CG_TRY(check_cuda(p, plan_malloc(&B.items, sizeof(int4) * cap_items), "cudaMalloc bins"));
     B.max_items = cap_items;
+    if (keys > 0) {
+      const int64_t cap_ii = keys + capM / kSubItem + 1;
+      CG_TRY(check_cuda(p, plan_malloc(&B.scount, sizeof(int32_t) * (keys + 1)), "cudaMalloc bins"));
+      CG_TRY(check_cuda(p, plan_malloc(&B.sub_off, sizeof(int32_t) * (keys + 1)), "cudaMalloc bins"));
+      CG_TRY(check_cuda(p, plan_malloc(&B.iitem_off, sizeof(int32_t) * (keys + 1)), "cudaMalloc bins"));
+      CG_TRY(check_cuda(p, plan_malloc(&B.iitems, sizeof(int4) * cap_ii), "cudaMalloc bins"));
+      B.max_iitems = cap_ii;
+    }
     p->bins_capacity_M = capM;
     p->bins_capacity_tiles = capT;
+    p->bins_capacity_keys = keys;
   }
   return CUNFFT_X_SUCCESS;
 }
@@ -798,6 +823,7 @@ int plan_autotune(Plan* p, int reps) {
   cudaGetLastError();
   if (best_T[0] == 0) {
     p->tl = best0;
+    p->it_ready = false;
     p->bins.valid = 0;
     return set_status(p, CUNFFT_X_CUDA_ERROR, "autotune: no candidate ran");
   }

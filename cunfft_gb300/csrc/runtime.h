@@ -39,6 +39,7 @@ struct Plan {
   Bins bins{};
   int64_t bins_capacity_M = -1;
   int64_t bins_capacity_tiles = -1;
+  int64_t bins_capacity_keys = -1;  // sub-bin keys the bins hold room for (Tiling::sub_on)
   const double* x = nullptr;   // device nodes of the current node set
   int64_t M = 0;
   int64_t* M_inst = nullptr;   // host copy of per-instance node counts
@@ -144,6 +145,9 @@ cudaError_t grid_launch_spread_tm(const Plan& p, const void* f, void* g, cudaStr
 // 2D tensor-core spreading kernel (grid_spread2_tm.cu); the tensor form runs it for 2D plans
 bool spread2_tm_supported(const Plan& p);
 cudaError_t grid_launch_spread2_tm(const Plan& p, const void* f, void* g, cudaStream_t st);
+// 2D tensor-core interpolation (grid_interp2_tc.cu): the sub-bins of a tiling it covers
+// (16 x 16 sub-tiles of window starts; Tiling::sub_on = 0 where it does not apply)
+void interp2_tc_subbins(const Plan& p, Tiling& tl);
 // tensor-core interpolation kernel (grid_interp_tc.cu)
 bool interp_tc_supported(const Plan& p);
 cudaError_t grid_launch_interp_tc(const Plan& p, const void* g, void* f, cudaStream_t st);

@@ -67,15 +67,15 @@ def _child(env_extra):
     return json.loads(r.stdout.strip().splitlines()[-1])
 
 
-# allocation k of one plan's life: 1-7 plan creation (roll-off table, grid, offsets,
-# counters, status, sample maximum), 8-16 node bins, 17-18 the tensor-core
+# allocation k of one plan's life: 1-8 plan creation (roll-off table, grid, offsets,
+# counters, item counts, status, sample maximum), 9-17 node bins, 18-19 the tensor-core
 # interpolation's split planes and their scales (first forward)
-@pytest.mark.parametrize("k", [1, 2, 7, 8, 12, 16, 17, 18])
+@pytest.mark.parametrize("k", [1, 2, 8, 9, 13, 17, 18, 19])
 def test_failed_allocation_is_a_status(k):
     from cunfft_gb300 import _native as nat
 
     out = _child({"CUNFFT_X_FAULT_ALLOC": str(k)})
-    if k >= 17:
+    if k >= 18:
         # the automatically chosen tensor-core interpolation falls back to the shared-tile
         # form when its buffers cannot be had: the transform still succeeds
         assert out["first"] in (nat.SUCCESS, nat.ALLOC_FAILED), out

@@ -152,7 +152,9 @@ def test_interp_kernel_selection_rules(dev):
     from cunfft_gb300._native import CunfftError
     from cunfft_gb300.nfft import NFFT
     x3 = torch.rand(100, 3, dtype=torch.float64, device=dev) - 0.5
-    for prec, N, x in (("f64", [16, 16, 16], x3), ("f32", [32, 32], x3[:, :2].contiguous()),
+    # FP64; a 2D grid whose inner tile is narrower than the 16-column sub-tiles; 3D with
+    # a last size below 8
+    for prec, N, x in (("f64", [16, 16, 16], x3), ("f32", [32, 4], x3[:, :2].contiguous()),
                        ("f32", [8, 8, 1], x3)):
         p = NFFT(N, precision=prec, device=dev).set_nodes(x)
         assert p.interp_kernel() == "shared"
@@ -162,6 +164,9 @@ def test_interp_kernel_selection_rules(dev):
         p.close()
     p = NFFT([16, 16, 16], m=8, precision="f32", device=dev).set_nodes(x3)   # 2m+2 = 18 > 16
     assert p.interp_kernel() == "shared"
+    p.close()
+    p = NFFT([32, 32], precision="f32", device=dev).set_nodes(x3[:, :2].contiguous())
+    assert p.interp_kernel() == "tensor"
     p.close()
     p = NFFT([32, 32, 32], precision="f32", device=dev).set_nodes(x3)
     assert p.interp_kernel() == "tensor"
