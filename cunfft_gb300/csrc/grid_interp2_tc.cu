@@ -35,7 +35,7 @@ void interp2_tc_subbins(const Plan& p, Tiling& tl) {
 bool interp2_tc_supported(const Plan& p) { return p.prec == kF32 && !p.tl.use_global && p.tl.sub_on; }
 
 // Split rows half [batch][4][P0][P2s], row scales float [batch][P0], and the 5-D map over
-// the rows (dims P2s, P0, 1, component, instance; box 32 halves x (S0 + W - 1) rows,
+// the rows (dims P2s, P0, 1, component, instance; box 32 halves x (16 + W - 1) rows,
 // 64-byte swizzle, zero fill outside).  Box rows are 64 bytes (32 halves); rows of the
 // arrays are multiples of 16 bytes (P2s % 8 == 0).
 cudaError_t interp2_tc_prepare(Plan& p, PFN_cuTensorMapEncodeTiled_v12000 enc) {
@@ -52,7 +52,7 @@ cudaError_t interp2_tc_prepare(Plan& p, PFN_cuTensorMapEncodeTiled_v12000 enc) {
       return e;
     }
   }
-  const int E0S = (1 << p.tl.ssh[0]) + p.geo.W - 1;
+  const int E0S = kI2Sub + p.geo.W - 1;  // rows of a 16-row sub-tile's windows (the kernel's B rows)
   const cuuint64_t dims[5] = {(cuuint64_t)sd.P2s, (cuuint64_t)sd.P0, 1u, 4u, (cuuint64_t)p.geo.batch};
   const cuuint64_t strides[4] = {(cuuint64_t)(sd.P2s * 2), (cuuint64_t)(comp * 2), (cuuint64_t)(comp * 2),
                                  (cuuint64_t)(4 * comp * 2)};

@@ -69,9 +69,11 @@ int main() {
     CHECK(L.b_off % 1024 == 0 && kI2Part % 512 == 0 && kI2Stage % 1024 == 0 && L.a_off % 1024 == 0 &&
               kItAPart % 1024 == 0 && L.bar_off % 16 == 0,
           "interp2: align (64-byte swizzle atoms, core matrices)");
-    CHECK(L.bar_off + 8u * (kI2Sets + 2 * kI2Stages + 2 * kI2Acc) + 8u <= L.total, "interp2: barriers");
+    CHECK(L.bar_off + 8u * (2 * kI2ABufs + 2 * kI2Stages + 2 * kI2Acc) + 8u <= L.total, "interp2: barriers");
     CHECK(kI2Acc * kI2N <= 512 && kI2N % 16 == 0 && kI2N <= 256, "interp2: tmem / MMA N");
-    CHECK(kI2Threads == (kI2NodeWarp0 + 4 * kI2Sets) * 32 && kI2Threads <= 1024, "interp2: roles");
+    CHECK(kI2Threads == (kI2RWarp0 + 4 * kI2Sets) * 32 && kI2Threads <= 1024 && kI2RWarp0 % 4 == 2 &&
+              kI2ABufs % kI2Sets == 0,
+          "interp2: roles");
     for (int W = 4; W <= 16; W += 2)
       CHECK(kI2Sub + W - 1 <= kI2K && kI2Sub + W - 1 <= kI2Rows && interp2_tc_ok(2, W, 64, 512) &&
                 !interp2_tc_ok(2, W, 8, 512) && !interp2_tc_ok(2, W, 64, 90),
