@@ -41,8 +41,10 @@ enum {
 };
 
 /** Interpolation (forward gridding) kernel.  AUTO picks TENSOR where it applies
- *  (d = 3, FP32, 2m+2 <= 16, outer tile extent <= 16, n_3 >= 4) and SHARED
- *  elsewhere; GLOBAL is reported when no shared-memory tile fits. */
+ *  (FP32, 2m+2 <= 16; in 3D an outer tile extent <= 16 and n_3 divisible by 8; in 2D an
+ *  inner tile extent >= 16 and n_2 divisible by 8, where the binning orders each tile's
+ *  nodes by 16 x 16 sub-tile) and SHARED elsewhere; GLOBAL is reported when no
+ *  shared-memory tile fits. */
 enum {
   CUNFFT_X_INTERP_AUTO = 0,
   CUNFFT_X_INTERP_SHARED = 1,   /* tile staged in shared memory, warp per node */
