@@ -119,11 +119,11 @@ __global__ void k_bin_scatter(const double* __restrict__ x, int64_t M, Geom geo,
 // totals are scanned in shared memory, and the round's total carries into the next.
 constexpr int kScanRound = 1024 * 8;
 
-__device__ __forceinline__ void warp_incl_scan2(int64_t& a, int64_t& b) {
+__device__ __forceinline__ void warp_incl_scan2(int32_t& a, int32_t& b) {
   const int lane = threadIdx.x & 31;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
-    const int64_t x = __shfl_up_sync(0xffffffffu, a, o), y = __shfl_up_sync(0xffffffffu, b, o);
+    const int32_t x = __shfl_up_sync(0xffffffffu, a, o), y = __shfl_up_sync(0xffffffffu, b, o);
     if (lane >= o) {
       a += x;
       b += y;
@@ -131,25 +131,27 @@ __device__ __forceinline__ void warp_incl_scan2(int64_t& a, int64_t& b) {
   }
 }
 
+// Positions and item counts fit 32 bits: the sorted arrays are int32-indexed.
 __global__ void __launch_bounds__(1024) k_scan_tiles(const int32_t* __restrict__ count, int64_t ntiles, int chunk,
                                                      int32_t* __restrict__ tile_off, int32_t* __restrict__ item_off,
                                                      int32_t* __restrict__ num_items) {
-  __shared__ int64_t wc[32], wi[32];
+  __shared__ int32_t wc[32], wi[32];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
   const int per = kScanRound / (int)blockDim.x;  // tiles per lane and round (8 at 1024 threads)
-  int64_t run_c = 0, run_i = 0;  // totals of the rounds before (the same in every thread)
+  const int csh = (chunk & (chunk - 1)) == 0 ? __ffs(chunk) - 1 : -1;  // chunk = 2^csh
+  int32_t run_c = 0, run_i = 0;  // totals of the rounds before (the same in every thread)
   for (int64_t r0 = 0; r0 < ntiles; r0 += kScanRound) {
     const int64_t wb = r0 + (int64_t)warp * 32 * per;
-    int64_t ec[8], ei[8], cc = 0, ci = 0;  // exclusive prefixes within the warp's tiles
+    int32_t ec[8], ei[8], cc = 0, ci = 0;  // exclusive prefixes within the warp's tiles
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
       const int64_t e = wb + 32 * k + lane;
       const int32_t v = (k < per && e < ntiles) ? count[e] : 0;
-      int64_t a = v, b = (v + chunk - 1) / chunk;
-      const int64_t v64 = a, w64 = b;
+      const int32_t w = csh >= 0 ? (v + chunk - 1) >> csh : (v + chunk - 1) / chunk;
+      int32_t a = v, b = w;
       warp_incl_scan2(a, b);
-      ec[k] = cc + a - v64;
-      ei[k] = ci + b - w64;
+      ec[k] = cc + a - v;
+      ei[k] = ci + b - w;
       cc += __shfl_sync(0xffffffffu, a, 31);
       ci += __shfl_sync(0xffffffffu, b, 31);
     }
@@ -159,19 +161,19 @@ __global__ void __launch_bounds__(1024) k_scan_tiles(const int32_t* __restrict__
     }
     __syncthreads();
     if (warp == 0) {
-      int64_t a = lane < nw ? wc[lane] : 0, b = lane < nw ? wi[lane] : 0;
+      int32_t a = lane < nw ? wc[lane] : 0, b = lane < nw ? wi[lane] : 0;
       warp_incl_scan2(a, b);
       wc[lane] = a;
       wi[lane] = b;
     }
     __syncthreads();
-    const int64_t bc = run_c + (warp > 0 ? wc[warp - 1] : 0), bi = run_i + (warp > 0 ? wi[warp - 1] : 0);
+    const int32_t bc = run_c + (warp > 0 ? wc[warp - 1] : 0), bi = run_i + (warp > 0 ? wi[warp - 1] : 0);
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
       const int64_t e = wb + 32 * k + lane;
       if (k < per && e < ntiles) {
-        tile_off[e] = (int32_t)(bc + ec[k]);
-        item_off[e] = (int32_t)(bi + ei[k]);
+        tile_off[e] = bc + ec[k];
+        item_off[e] = bi + ei[k];
       }
     }
     run_c += wc[nw - 1];
@@ -179,9 +181,9 @@ __global__ void __launch_bounds__(1024) k_scan_tiles(const int32_t* __restrict__
     __syncthreads();  // wc / wi are rewritten by the next round
   }
   if (tid == 0) {
-    tile_off[ntiles] = (int32_t)run_c;
-    item_off[ntiles] = (int32_t)run_i;
-    *num_items = (int32_t)run_i;
+    tile_off[ntiles] = run_c;
+    item_off[ntiles] = run_i;
+    *num_items = run_i;
   }
 }
 
