@@ -156,7 +156,7 @@ int cunfft_x_spread(cunfft_x_plan *plan, const void *f, void *g);
  *  n = 256^3 needs 16384 or 32768 tiles and fits, n = 512^3 does not; wider windows
  *  (m >= 8) use 8 x 4 x 8 (FP32) or 4 x 4 x 8 (FP64) tiles in 3D, and a tile whose
  *  padded copy would not fit shared memory is halved along dimension 0.  2D tiles
- *  are 32 x 64 grid points, 1D tiles 2048.
+ *  are 64 x 64 grid points (FP32, m <= 7) or 32 x 64, 1D tiles 2048.
  *  Larger requests return CUNFFT_X_INVALID_ARGUMENT with a message on stderr and
  *  do no device work.  M = 0 leaves g unchanged.
  *
