@@ -131,11 +131,13 @@ struct Tiling {
   int use_global;        // 1: no shared-memory tile fits, grid in global memory
   int spread_kernel;     // spreading kernel in use: CUNFFT_X_SPREAD_SHARED, _REGISTER, _TENSOR or _GLOBAL
   int interp_kernel;     // interpolation kernel in use: CUNFFT_X_INTERP_SHARED, _TENSOR or _GLOBAL
-  // Sub-bins (2D FP32 plans the tensor-core interpolation covers, sub_on = 1): the
-  // counting sort orders the nodes of a tile by sub-tile of 2^ssh[0] x 2^ssh[1] window
-  // starts, sub-bin (s0, s1) = s0 snb1 + s1 of ns per tile, and the binning also makes the
-  // sub-bins' interpolation items; sub_on = 0: tile order only (ns = 1)
+  // Sub-bins (sub_on = 1): the counting sort orders the nodes of a tile by sub-bin of
+  // 2^ssh[0] x 2^ssh[1] window starts (dimensions 0 and 1), sub-bin (s0, s1) = s0 snb1 + s1
+  // of ns per tile.  2D FP32 plans the tensor-core interpolation covers take 16 x 16
+  // sub-tiles, and the binning also makes their interpolation items (sub_items = 1).
+  // sub_on = 0: tile order only (ns = 1).
   int sub_on;
+  int sub_items;
   int ns;
   int ssh[2];
   int snb1;
@@ -159,8 +161,10 @@ struct Bins {
   uint32_t* fmax;        // [1] largest |Re|, |Im| of the samples being spread (float bits), per call
   // sub-bins (Tiling::sub_on): the counting sort's key is tile * ns + sub-bin
   int32_t* scount;       // [tiles_total * ns + 1] nodes per sub-bin
-  int32_t* sub_off;      // [tiles_total * ns + 1] exclusive scan of scount: first sorted node of each sub-bin
-  int32_t* iitem_off;    // [tiles_total * ns + 1] exclusive scan of the sub-bins' interpolation items
+  int32_t* sub_pre;      // [tiles_total * ns] nodes of the tile's sub-bins before this one
+  int32_t* icount;       // [tiles_total + 1] interpolation items per tile (Tiling::sub_items)
+  int32_t* iitem_off;    // [tiles_total + 1] exclusive scan of icount
+  int32_t* iscratch;     // [tiles_total + 1] the scan's second output, unused
   int4*    iitems;       // [max_iitems] (sub-bin key, start, end, 0): at most kSubItem nodes of one sub-tile
   int32_t* num_iitems;   // [1]
   int64_t  max_iitems;

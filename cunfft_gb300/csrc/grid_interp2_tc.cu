@@ -18,6 +18,7 @@ static int log2_of(int v) {
 // the binning sorts every tile's nodes by, for a 2D FP32 tiling this kernel covers.
 void interp2_tc_subbins(const Plan& p, Tiling& tl) {
   tl.sub_on = 0;
+  tl.sub_items = 0;
   tl.ns = 1;
   tl.ssh[0] = tl.ssh[1] = 0;
   tl.snb1 = 1;
@@ -30,9 +31,12 @@ void interp2_tc_subbins(const Plan& p, Tiling& tl) {
   tl.snb1 = tl.T[1] / kI2Sub;
   tl.ns = ns;
   tl.sub_on = 1;
+  tl.sub_items = 1;
 }
 
-bool interp2_tc_supported(const Plan& p) { return p.prec == kF32 && !p.tl.use_global && p.tl.sub_on; }
+bool interp2_tc_supported(const Plan& p) {
+  return p.geo.d == 2 && p.prec == kF32 && !p.tl.use_global && p.tl.sub_on && p.tl.sub_items;
+}
 
 // Split rows half [batch][4][P0][P2s], row scales float [batch][P0], and the 5-D map over
 // the rows (dims P2s, P0, 1, component, instance; box 32 halves x (16 + W - 1) rows,

@@ -79,14 +79,18 @@ __global__ void k_bin_count(const double* __restrict__ x, int64_t M, Geom geo, T
 // FP32 fractions on power-of-two sizes come from the integer form: the exact c - m
 // rounded once to FP32 (the FP64 form rounds c to FP64 first; the two differ by at most
 // one FP32 ulp plus 2^-49).  FP64 fractions always take the FP64 form.
+// With sub-bins the key is tile * ns + sub-bin (ns a power of two): the node's place is its
+// tile's first place, then the tile's sub-bins before its own, then its rank.
 template <typename T>
 __global__ void k_bin_scatter(const double* __restrict__ x, int64_t M, Geom geo, Tiling tl, BinLog2 lg,
                               const int2* __restrict__ tile_rank, const int32_t* __restrict__ tile_off,
-                              int32_t* __restrict__ sidx, int32_t* __restrict__ soff, T* __restrict__ sfrac) {
+                              const int32_t* __restrict__ sub_pre, int32_t* __restrict__ sidx,
+                              int32_t* __restrict__ soff, T* __restrict__ sfrac) {
   const int d = geo.d;
+  const int nsh = __ffs(tl.ns) - 1;  // ns = 2^nsh
   for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < M; j += (int64_t)gridDim.x * blockDim.x) {
     int2 tr = tile_rank[j];
-    int64_t pos = (int64_t)tile_off[tr.x] + tr.y;
+    int64_t pos = tl.sub_on ? (int64_t)tile_off[tr.x >> nsh] + sub_pre[tr.x] + tr.y : (int64_t)tile_off[tr.x] + tr.y;
     uint32_t packed = 0;
     for (int t = 0; t < d; ++t) {
       const double xt = x[j * d + t];
@@ -187,11 +191,38 @@ __global__ void __launch_bounds__(1024) k_scan_tiles(const int32_t* __restrict__
   }
 }
 
-// Nodes per tile from the sub-bin offsets (sub-bins of a tile are consecutive keys).
-__global__ void k_tile_counts(const int32_t* __restrict__ sub_off, int64_t ntiles, int ns,
-                              int32_t* __restrict__ count) {
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < ntiles; t += (int64_t)gridDim.x * blockDim.x)
-    count[t] = sub_off[(t + 1) * ns] - sub_off[t * ns];
+// Per tile from its sub-bin counts (the tile's ns consecutive keys): the tile's node
+// count, each sub-bin's place inside the tile, and the tile's interpolation items of at
+// most kSubItem nodes of one sub-bin (with sub_items).
+__global__ void k_tile_subs(const int32_t* __restrict__ scount, int64_t ntiles, int ns, int sub_items,
+                            int32_t* __restrict__ count, int32_t* __restrict__ sub_pre, int32_t* __restrict__ icount) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < ntiles; t += (int64_t)gridDim.x * blockDim.x) {
+    int32_t c = 0, ic = 0;
+    for (int s = 0; s < ns; ++s) {
+      const int32_t v = scount[t * ns + s];
+      sub_pre[t * ns + s] = c;
+      c += v;
+      ic += (v + kSubItem - 1) / kSubItem;
+    }
+    count[t] = c;
+    if (sub_items) icount[t] = ic;
+  }
+}
+
+// The interpolation items of each sub-bin, kSubItem nodes at a time (thread per sub-bin:
+// its first item follows the items of its tile's sub-bins before it).
+__global__ void k_make_sub_items(const int32_t* __restrict__ scount, const int32_t* __restrict__ sub_pre,
+                                 const int32_t* __restrict__ tile_off, const int32_t* __restrict__ iitem_off,
+                                 int64_t nkeys, int ns, int4* __restrict__ iitems) {
+  for (int64_t key = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; key < nkeys;
+       key += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t t = key / ns, k0 = t * ns;
+    int32_t io = iitem_off[t];
+    for (int64_t q = k0; q < key; ++q) io += (scount[q] + kSubItem - 1) / kSubItem;
+    const int32_t c = scount[key], a0 = tile_off[t] + sub_pre[key];
+    for (int32_t k = 0; k * kSubItem < c; ++k, ++io)
+      iitems[io] = make_int4((int)key, a0 + k * kSubItem, min(a0 + c, a0 + (k + 1) * kSubItem), 0);
+  }
 }
 
 __global__ void k_make_items(const int32_t* __restrict__ count, const int32_t* __restrict__ tile_off,
@@ -225,37 +256,36 @@ cudaError_t launch_binning(const Plan& p, const double* x, cudaStream_t st) {
       }
     lg.k[t] = k;
   }
-  // counting sort over keys: tiles, or tile * ns + sub-bin with sub-bins; the positions
-  // come from the scan of the key counts, the tile-level items from the tile counts
+  // counting sort over keys: tiles, or tile * ns + sub-bin with sub-bins; the tile counts
+  // then come from the sub-bin counts, and only the tiles are scanned
   const bool sub = tl.sub_on != 0;
   const int64_t nkeys = tl.tiles_total * (sub ? tl.ns : 1);
   int32_t* kcount = sub ? B.scount : B.count;
-  int32_t* koff = sub ? B.sub_off : B.tile_off;
   cudaError_t e = cudaMemsetAsync(kcount, 0, sizeof(int32_t) * (nkeys + 1), st);
   if (e != cudaSuccess) return e;
   if (B.M > 0) {
     k_bin_count<<<grid_for(B.M, 256, p.num_sms), 256, 0, st>>>(x, B.M, p.geo, tl, lg, B.inst_off, kcount,
                                                                  B.tile_rank);
   }
-  if (sub) {
-    // sub-bin offsets and the interpolation items of at most kSubItem nodes per sub-bin
-    k_scan_tiles<<<1, 1024, 0, st>>>(B.scount, nkeys, kSubItem, B.sub_off, B.iitem_off, B.num_iitems);
-    k_tile_counts<<<grid_for(tl.tiles_total, 256, p.num_sms), 256, 0, st>>>(B.sub_off, tl.tiles_total, tl.ns,
-                                                                             B.count);
-  }
+  if (sub)
+    k_tile_subs<<<grid_for(tl.tiles_total, 256, p.num_sms), 256, 0, st>>>(B.scount, tl.tiles_total, tl.ns,
+                                                                           tl.sub_items, B.count, B.sub_pre,
+                                                                           B.icount);
   k_scan_tiles<<<1, 1024, 0, st>>>(B.count, tl.tiles_total, tl.chunk, B.tile_off, B.item_off, B.num_items);
+  if (sub && tl.sub_items)  // chunk 1: the scan of the item counts themselves
+    k_scan_tiles<<<1, 1024, 0, st>>>(B.icount, tl.tiles_total, 1, B.iitem_off, B.iscratch, B.num_iitems);
   if (B.M > 0) {
     if (p.prec == kF64)
       k_bin_scatter<double><<<grid_for(B.M, 256, p.num_sms), 256, 0, st>>>(
-          x, B.M, p.geo, tl, lg, B.tile_rank, koff, B.sidx, B.soff, (double*)B.sfrac);
+          x, B.M, p.geo, tl, lg, B.tile_rank, B.tile_off, B.sub_pre, B.sidx, B.soff, (double*)B.sfrac);
     else
       k_bin_scatter<float><<<grid_for(B.M, 256, p.num_sms), 256, 0, st>>>(
-          x, B.M, p.geo, tl, lg, B.tile_rank, koff, B.sidx, B.soff, (float*)B.sfrac);
+          x, B.M, p.geo, tl, lg, B.tile_rank, B.tile_off, B.sub_pre, B.sidx, B.soff, (float*)B.sfrac);
     k_make_items<<<grid_for(tl.tiles_total, 256, p.num_sms), 256, 0, st>>>(B.count, B.tile_off, B.item_off,
                                                                             tl.tiles_total, tl.chunk, B.items);
-    if (sub)
-      k_make_items<<<grid_for(nkeys, 256, p.num_sms), 256, 0, st>>>(B.scount, B.sub_off, B.iitem_off, nkeys,
-                                                                      kSubItem, B.iitems);
+    if (sub && tl.sub_items)
+      k_make_sub_items<<<grid_for(nkeys, 256, p.num_sms), 256, 0, st>>>(B.scount, B.sub_pre, B.tile_off,
+                                                                          B.iitem_off, nkeys, tl.ns, B.iitems);
   }
   return cudaGetLastError();
 }

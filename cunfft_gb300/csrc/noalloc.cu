@@ -109,6 +109,7 @@ extern "C" int cunfft_x_spread_noalloc(int d, const int64_t* N, const int64_t* n
     return s;
   }
   p.tl.sub_on = 0;  // spreading needs the nodes in tile order only: no sub-bins, no room for them
+  p.tl.sub_items = 0;
   p.tl.ns = 1;
   if (p.tl.tiles_total > kNaMaxTiles) {
     fprintf(stderr, "cunfft_x_spread_noalloc: the grid needs %lld tiles, beyond the fixed scratch limit of %lld\n",

@@ -83,12 +83,15 @@ static void free_bins(Plan* p) {
   cudaFree(B.item_off);
   cudaFree(B.items);
   cudaFree(B.scount);
-  cudaFree(B.sub_off);
+  cudaFree(B.sub_pre);
+  cudaFree(B.icount);
   cudaFree(B.iitem_off);
+  cudaFree(B.iscratch);
   cudaFree(B.iitems);
   B.sidx = nullptr; B.soff = nullptr; B.sfrac = nullptr; B.tile_rank = nullptr; B.fperm = nullptr;
   B.count = nullptr; B.tile_off = nullptr; B.item_off = nullptr; B.items = nullptr;
-  B.scount = nullptr; B.sub_off = nullptr; B.iitem_off = nullptr; B.iitems = nullptr;
+  B.scount = nullptr; B.sub_pre = nullptr; B.icount = nullptr; B.iitem_off = nullptr; B.iscratch = nullptr;
+  B.iitems = nullptr;
   B.max_iitems = 0;
   p->bins_capacity_M = -1;
   p->bins_capacity_tiles = -1;
@@ -147,6 +150,7 @@ static Tiling make_tiling(const Plan* p, const int* T, int chunk) {
   const bool t2 = d == 2 && p->prec == kF32 && W <= 16;
   tl.chunk = chunk > 0 ? chunk : (d == 3 ? 1024 : (t2 ? 256 : 2048));
   tl.use_global = 0;
+  tl.ns = 1;  // no sub-bins unless the plan asks for them (plan_choose_tiling)
   return tl;
 }
 
@@ -513,7 +517,7 @@ static int ensure_bins(Plan* p, int64_t M) {
   const int64_t max_items = tiles + M / std::max(1, p->tl.chunk) + 1;
   // sub-bin keys and their interpolation items (each sub-bin: at most count / kSubItem + 1)
   const int64_t keys = p->tl.sub_on ? tiles * p->tl.ns : 0;
-  const int64_t max_iitems = keys > 0 ? keys + M / kSubItem + 1 : 0;
+  const int64_t max_iitems = keys > 0 && p->tl.sub_items ? keys + M / kSubItem + 1 : 0;
   const size_t real = elem_bytes(p) / 2;
   if (M > p->bins_capacity_M || tiles > p->bins_capacity_tiles || max_items > B.max_items ||
       keys > p->bins_capacity_keys || max_iitems > B.max_iitems || p->bins_capacity_M < 0) {
@@ -531,10 +535,14 @@ static int ensure_bins(Plan* p, int64_t M) {
     CG_TRY(check_cuda(p, plan_malloc(&B.items, sizeof(int4) * cap_items), "cudaMalloc bins"));
     B.max_items = cap_items;
     if (keys > 0) {
-      const int64_t cap_ii = keys + capM / kSubItem + 1;
       CG_TRY(check_cuda(p, plan_malloc(&B.scount, sizeof(int32_t) * (keys + 1)), "cudaMalloc bins"));
-      CG_TRY(check_cuda(p, plan_malloc(&B.sub_off, sizeof(int32_t) * (keys + 1)), "cudaMalloc bins"));
-      CG_TRY(check_cuda(p, plan_malloc(&B.iitem_off, sizeof(int32_t) * (keys + 1)), "cudaMalloc bins"));
+      CG_TRY(check_cuda(p, plan_malloc(&B.sub_pre, sizeof(int32_t) * keys), "cudaMalloc bins"));
+    }
+    if (max_iitems > 0) {
+      const int64_t cap_ii = keys + capM / kSubItem + 1;
+      CG_TRY(check_cuda(p, plan_malloc(&B.icount, sizeof(int32_t) * (capT + 1)), "cudaMalloc bins"));
+      CG_TRY(check_cuda(p, plan_malloc(&B.iitem_off, sizeof(int32_t) * (capT + 1)), "cudaMalloc bins"));
+      CG_TRY(check_cuda(p, plan_malloc(&B.iscratch, sizeof(int32_t) * (capT + 1)), "cudaMalloc bins"));
       CG_TRY(check_cuda(p, plan_malloc(&B.iitems, sizeof(int4) * cap_ii), "cudaMalloc bins"));
       B.max_iitems = cap_ii;
     }
