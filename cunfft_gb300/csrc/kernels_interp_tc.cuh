@@ -178,7 +178,9 @@ static __global__ void __launch_bounds__(kItSplitThreads) k_split_planes(const f
     const float scale = ldexpf(1.f, kItLogB - ex);
     if (threadIdx.x == 0) inv_scale[inst * sd.P0 + i0] = ldexpf(1.f, ex - kItLogB);
     __half* const o_plane = out + inst * 4 * comp + i0 * sd.P1 * sd.P2s;
-    for (int64_t e = threadIdx.x; e < sd.P1 * q4; e += blockDim.x) {
+    // the second pass runs backwards: the plane's last lines, read most recently, are the
+    // likeliest still in L2
+    for (int64_t e = sd.P1 * q4 - 1 - threadIdx.x; e >= 0; e -= blockDim.x) {
       const int64_t i1 = e / q4, i2 = (e - i1 * q4) * 4;
       float4 a, b;
       ld_quad(src + wrap_up(i1, geo.n[1]) * geo.n[2] + wrap_up(i2, geo.n[2]), al16, a, b);
