@@ -205,20 +205,40 @@ __global__ void __launch_bounds__(kT2Threads, 1) k_spread2_tm(const float2* __re
       const unsigned char* sl = smem + L.rec_off + r * kT2SlotBytes;
       const uint32_t* offs = reinterpret_cast<const uint32_t*>(sl + kT2SlotOff);
       const float2* frs = reinterpret_cast<const float2*>(sl + kT2SlotFrac);
+      // Does any node of the batch reach this warp's rows (A: p0 in [32 lw, 32 lw + 32)) or
+      // columns (B: p1 in [16 b, 16 b + 16), b = lw - 4)?  Node j reaches [o_j, o_j + W).  With the
+      // binning's 16 x 16 sub-tile order a batch's window starts lie within a few rows and
+      // columns, so most operand warps of a batch only write zeros; the test is
+      // warp-uniform, and a warp that is reached computes exactly what it did before.
+      bool reached;
+      {
+        const uint32_t mo = offs[lane & (kTcK - 1)];
+        const bool has = lane < kTcK && mo != 0xffffffffu;
+        const uint32_t o = is_a ? (mo & MASK) : ((mo >> SH) & MASK);
+        const uint32_t omin = __reduce_min_sync(0xffffffffu, has ? o : 0xffffffffu);
+        const uint32_t oend = __reduce_max_sync(0xffffffffu, has ? o + (uint32_t)W : 0u);  // 0: no node
+        const int r0 = is_a ? 32 * lw : 16 * (lw - kT2AWarps), rn = is_a ? 32 : 16;
+        reached = oend != 0u && (int)omin < r0 + rn && (int)oend > r0;
+      }
       if (is_a) {
         tc::fence_after_sync();
         uint32_t hi[8], lo[8];
+        if (reached) {
 #pragma unroll
-        for (int c = 0; c < 8; ++c) {
-          float v[2];
+          for (int c = 0; c < 8; ++c) {
+            float v[2];
 #pragma unroll
-          for (int u = 0; u < 2; ++u) {
-            const int j = 2 * c + u;
-            const uint32_t off = offs[j];
-            const int l = p0 - (int)(off & MASK);  // no node: l < 0, a zero tap
-            v[u] = tc_tap<WIN>(frs[j].x, mf, l, W, k0) * kTcScaleA;
+            for (int u = 0; u < 2; ++u) {
+              const int j = 2 * c + u;
+              const uint32_t off = offs[j];
+              const int l = p0 - (int)(off & MASK);  // no node: l < 0, a zero tap
+              v[u] = tc_tap<WIN>(frs[j].x, mf, l, W, k0) * kTcScaleA;
+            }
+            tc_split2_f16(make_float2(v[0], v[1]), hi[c], lo[c]);
           }
-          tc_split2_f16(make_float2(v[0], v[1]), hi[c], lo[c]);
+        } else {
+#pragma unroll
+          for (int c = 0; c < 8; ++c) hi[c] = lo[c] = 0u;
         }
         const uint32_t ta = tmem + ((uint32_t)(32 * lw) << 16) + kT2ACol0 + st * 16u;
         tc::tmem_st8(ta, hi);
@@ -227,20 +247,24 @@ __global__ void __launch_bounds__(kT2Threads, 1) k_spread2_tm(const float2* __re
         tc::fence_before_sync();
       } else {
         const float2* val = reinterpret_cast<const float2*>(sl + kT2SlotVal);
-        float re[8], im[8];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-          const int j = 8 * h + u;
-          const uint32_t off = offs[j];
-          const int l = off == 0xffffffffu ? -1 : p1 - (int)((off >> SH) & MASK);
-          const float w = tc_tap<WIN>(frs[j].y, mf, l, W, k1) * bscale;
-          const float2 v = val[j];
-          re[u] = w * v.x;
-          im[u] = w * v.y;
-        }
         uint4 rh, rl, ih, il;
-        tc_split8_f16(re, rh, rl);
-        tc_split8_f16(im, ih, il);
+        if (reached) {
+          float re[8], im[8];
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            const int j = 8 * h + u;
+            const uint32_t off = offs[j];
+            const int l = off == 0xffffffffu ? -1 : p1 - (int)((off >> SH) & MASK);
+            const float w = tc_tap<WIN>(frs[j].y, mf, l, W, k1) * bscale;
+            const float2 v = val[j];
+            re[u] = w * v.x;
+            im[u] = w * v.y;
+          }
+          tc_split8_f16(re, rh, rl);
+          tc_split8_f16(im, ih, il);
+        } else {
+          rh = rl = ih = il = make_uint4(0u, 0u, 0u, 0u);
+        }
         unsigned char* bst = smem + L.b_off + st * 2u * kT2BBytes;
         const int r0 = 2 * p1;  // rows r0 (Re) and r0 + 1 (Im): same 8-row group
         const uint32_t o0 = tc_elem_off(r0 >> 3, r0 & 7, h), o1 = tc_elem_off(r0 >> 3, (r0 & 7) + 1, h);
