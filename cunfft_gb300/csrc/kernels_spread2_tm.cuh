@@ -54,7 +54,7 @@ constexpr int kT2Threads = (kT2OpSet1 + kT2OpWarps) * 32;
 constexpr int kT2Stages = 4;
 constexpr int kT2Ring = 8;                 // record slots
 constexpr int kT2Ahead = 4;                // record loads in flight (batches)
-constexpr uint32_t kT2Spin = 64;           // non-blocking polls before a hand-off wait suspends
+constexpr uint32_t kT2Spin = 8;            // non-blocking polls before a hand-off wait suspends
 constexpr uint32_t kT2BBytes = (uint32_t)kT2N * kTcK * 2u;   // one FP16 part of one B stage
 constexpr uint32_t kT2ACol0 = 2u * kT2N;   // A stages after the two accumulator sets
 constexpr int kT2StgStride = kT2N + 4;     // floats per staging row
