@@ -9,7 +9,7 @@ uniform [-1, 1] (seeded synthetic data; the reference publishes no dataset).
 A step = bind the node set (FP64 node reduction + binning) + forward NFFT +
 adjoint NFFT, i.e. one pass of the hot path over one batch of nodes;
 value = M * n_gpus / (time per step), max over ranks.  ``value`` is the FP32
-form (FP32 gridding, FFT, roll-off and accumulation; FP64 node reduction);
+form (FP32 gridding, FFT and accumulation; FP64 node reduction and roll-off);
 the FP64 form (the reference's arithmetic) is timed in the same run and
 reported as ``fp64_plain``.  Errors are relative l2 against the FP64 direct
 NDFT on a 4096-node subsample (forward) and 4096 coefficients (adjoint).  The
@@ -576,8 +576,8 @@ def run_ours(args):
         "steps": args.steps, "warmup": warm, "ms_per_step": ms32_max,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "c64: gridding on tcgen05 kind::f16 with FP16 hi/lo operands, three products "
-                 "(hi*hi + hi*lo + lo*hi) per tap, FP32 accumulate; FP32 FFT and roll-off; FP64 node reduction "
-                 "(integer arithmetic on power-of-two grids)",
+                 "(hi*hi + hi*lo + lo*hi) per tap, FP32 accumulate; FP32 FFT; FP64 node reduction and "
+                 "roll-off factors",
         "data": "synthetic (seeded uniform nodes and coefficients, the reference's 3D workload shape)",
         "config": {"workload": "3D NFFT fwd+adj, N=128^3, n=256^3 (sigma=2), Gaussian m=6, M=2^21 uniform nodes",
                    "step": "bin nodes + forward + adjoint", "form": "FP32", "parallelism": f"replicas x{world}",

@@ -5,24 +5,12 @@
 // written as one pass over the whole grid (no separate memset).
 // Adjoint  (src/cunfft_kernel.cu:264-275, 318-343, 418-467):
 //   f_hat[k] = g[k mod n] * prod_t exp(fac_t k_t^2).
-// fac_t = pi^2 b_t / n_t^2 (src/cunfft.cu:87).  The FP64 form multiplies the FP64
-// factors; the FP32 form multiplies the factors rounded to FP32, in FP32 (FP64
-// arithmetic runs at a small fraction of the FP32 rate on this GPU): its factor product
-// carries d roundings of the table and d - 1 of the products, at most (2d - 1) / 2 FP32
-// ulp.  Frequencies run over k_t in [-floor(N_t/2), N_t - floor(N_t/2)).
+// fac_t = pi^2 b_t / n_t^2 (src/cunfft.cu:87).  The factor tables are FP64 in both
+// forms; the FP32 form multiplies the FP64 factor product, rounded once, into
+// FP32 data.  Frequencies run over k_t in [-floor(N_t/2), N_t - floor(N_t/2)).
 #include "runtime.h"
 
 namespace cg {
-
-// the factors' type: FP64 for the FP64 form, FP32 for the FP32 form
-template <typename T>
-struct RocReal {
-  using t = double;
-};
-template <>
-struct RocReal<float> {
-  using t = float;
-};
 
 // log2 of the grid sizes when every one is a power of two, computed on the host
 struct RocShifts {
@@ -41,13 +29,12 @@ __device__ __forceinline__ int64_t roc_slot(int64_t i, int64_t N, int64_t n) {
 
 // EPT consecutive grid points per thread (2 when the last grid size is even, so a
 // pair never leaves its row; 1 otherwise); integer decoding by shifts and masks when
-// every grid size is a power of two (P2), by division otherwise, and the factor
+// every grid size is a power of two (P2), by division otherwise, and the FP64 factor
 // product, in the order dimension 0, 1, ..., only for points inside I_N.
 template <typename T, int EPT, bool P2>
 __global__ void k_roc_forward(const typename Cx<T>::t* __restrict__ fhat, typename Cx<T>::t* __restrict__ g,
-                              Geom geo, const typename RocReal<T>::t* __restrict__ tab, RocShifts sh) {
+                              Geom geo, const double* __restrict__ tab, RocShifts sh) {
   using C = typename Cx<T>::t;
-  using R = typename RocReal<T>::t;
   const int d = geo.d;
   const int64_t total2 = geo.ntot * geo.batch / EPT;
   const int64_t n_last = geo.n[d - 1], N_last = geo.N[d - 1];
@@ -72,7 +59,7 @@ __global__ void k_roc_forward(const typename Cx<T>::t* __restrict__ fhat, typena
     }
     bool lead_in = true;
     int64_t ci = 0, tab_base = 0;
-    R fac = (R)1;
+    double fac = 1.0;
     for (int t = 0; t < d - 1 && lead_in; ++t) {
       const int64_t c = roc_slot(lead_idx[t], geo.N[t], geo.n[t]);
       if (c < 0) {
@@ -104,9 +91,8 @@ __global__ void k_roc_forward(const typename Cx<T>::t* __restrict__ fhat, typena
 // Coefficient crop; 32-bit index arithmetic when the coefficient count allows it.
 template <typename T, typename I>
 __global__ void k_roc_adjoint(const typename Cx<T>::t* __restrict__ g, typename Cx<T>::t* __restrict__ fhat,
-                              Geom geo, const typename RocReal<T>::t* __restrict__ tab) {
+                              Geom geo, const double* __restrict__ tab) {
   using C = typename Cx<T>::t;
-  using R = typename RocReal<T>::t;
   const int d = geo.d;
   const I Ntot = (I)geo.Ntot;
   const I total = Ntot * (I)geo.batch;
@@ -120,7 +106,7 @@ __global__ void k_roc_adjoint(const typename Cx<T>::t* __restrict__ g, typename 
       c[t] = rem - q * Nt;
       rem = q;
     }
-    R fac = (R)1;
+    double fac = 1.0;
     int64_t gidx = 0, tab_base = 0;
     for (int t = 0; t < d; ++t) {
       const int64_t k = (int64_t)c[t] - geo.N[t] / 2;
@@ -162,29 +148,16 @@ static inline int roc_grid(const Plan& p, int64_t work) {
   return (int)(b > cap ? cap : (b < 1 ? 1 : b));
 }
 
-// the plan's factor table for the form computing in T
-template <typename T>
-static const typename RocReal<T>::t* roc_table(const Plan& p);
-template <>
-const double* roc_table<double>(const Plan& p) {
-  return p.roc_tab;
-}
-template <>
-const float* roc_table<float>(const Plan& p) {
-  return p.roc_tab32;
-}
-
 template <typename T>
 static cudaError_t launch_roc_fwd_t(const Plan& p, bool pairs, bool p2, int blocks, const void* fhat, void* g,
                                    const RocShifts& sh, cudaStream_t st) {
   using C = typename Cx<T>::t;
   const C* in = (const C*)fhat;
   C* out = (C*)g;
-  const typename RocReal<T>::t* tab = roc_table<T>(p);
-  if (pairs && p2) k_roc_forward<T, 2, true><<<blocks, 256, 0, st>>>(in, out, p.geo, tab, sh);
-  else if (pairs) k_roc_forward<T, 2, false><<<blocks, 256, 0, st>>>(in, out, p.geo, tab, sh);
-  else if (p2) k_roc_forward<T, 1, true><<<blocks, 256, 0, st>>>(in, out, p.geo, tab, sh);
-  else k_roc_forward<T, 1, false><<<blocks, 256, 0, st>>>(in, out, p.geo, tab, sh);
+  if (pairs && p2) k_roc_forward<T, 2, true><<<blocks, 256, 0, st>>>(in, out, p.geo, p.roc_tab, sh);
+  else if (pairs) k_roc_forward<T, 2, false><<<blocks, 256, 0, st>>>(in, out, p.geo, p.roc_tab, sh);
+  else if (p2) k_roc_forward<T, 1, true><<<blocks, 256, 0, st>>>(in, out, p.geo, p.roc_tab, sh);
+  else k_roc_forward<T, 1, false><<<blocks, 256, 0, st>>>(in, out, p.geo, p.roc_tab, sh);
   return cudaGetLastError();
 }
 
@@ -207,9 +180,9 @@ cudaError_t launch_roc_adjoint(const Plan& p, const void* g, void* fhat, cudaStr
       k_roc_adjoint<double, int64_t><<<roc_grid(p, work), 256, 0, st>>>((const double2*)g, (double2*)fhat, p.geo, p.roc_tab);
   } else {
     if (small)
-      k_roc_adjoint<float, uint32_t><<<roc_grid(p, work), 256, 0, st>>>((const float2*)g, (float2*)fhat, p.geo, p.roc_tab32);
+      k_roc_adjoint<float, uint32_t><<<roc_grid(p, work), 256, 0, st>>>((const float2*)g, (float2*)fhat, p.geo, p.roc_tab);
     else
-      k_roc_adjoint<float, int64_t><<<roc_grid(p, work), 256, 0, st>>>((const float2*)g, (float2*)fhat, p.geo, p.roc_tab32);
+      k_roc_adjoint<float, int64_t><<<roc_grid(p, work), 256, 0, st>>>((const float2*)g, (float2*)fhat, p.geo, p.roc_tab);
   }
   return cudaGetLastError();
 }

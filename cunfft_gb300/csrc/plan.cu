@@ -396,19 +396,6 @@ int geom_init(Plan* p, int d, const int64_t* N, const int64_t* n, int m, int pre
 
 int plan_window(const Plan* p) { return p->geo.window; }
 
-// The roll-off table on the device: sum_t N_t doubles, then the same factors rounded to
-// FP32 for the FP32 form, whose kernels multiply them in FP32 (FP64 arithmetic runs at a
-// small fraction of the FP32 rate on this GPU).
-static cudaError_t upload_roc(Plan* p, const std::vector<double>& tab) {
-  std::vector<unsigned char> buf(tab.size() * (sizeof(double) + sizeof(float)));
-  memcpy(buf.data(), tab.data(), sizeof(double) * tab.size());
-  for (size_t i = 0; i < tab.size(); ++i) {
-    const float v = (float)tab[i];
-    memcpy(buf.data() + sizeof(double) * tab.size() + sizeof(float) * i, &v, sizeof(float));
-  }
-  return cudaMemcpy(p->roc_tab, buf.data(), buf.size(), cudaMemcpyHostToDevice);
-}
-
 // Switch the window: new tap constants and roll-off factors (same table size);
 // captured graphs hold the old constants by value and are re-captured.
 int plan_set_window(Plan* p, int window) {
@@ -418,7 +405,8 @@ int plan_set_window(Plan* p, int window) {
     CG_TRY(check_cuda(p, cudaStreamSynchronize(p->stream), "cudaStreamSynchronize"));  // the old table may be in use
     window_constants(p->geo, window);
     const std::vector<double> tab = roc_factors(p->geo);
-    CG_TRY(check_cuda(p, upload_roc(p, tab), "upload roll-off table"));
+    CG_TRY(check_cuda(p, cudaMemcpy(p->roc_tab, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice),
+                      "upload roll-off table"));
     ++p->node_gen;
   }
   return set_status(p, CUNFFT_X_SUCCESS, nullptr);
@@ -440,10 +428,9 @@ int plan_init(Plan* p, int d, const int64_t* N, const int64_t* n, int m, int pre
   // roll-off factor tables, per dimension
   {
     const std::vector<double> tab = roc_factors(g);
-    CG_TRY(check_cuda(p, plan_malloc(&p->roc_tab, (sizeof(double) + sizeof(float)) * tab.size()),
-                      "cudaMalloc roll-off table"));
-    p->roc_tab32 = reinterpret_cast<float*>(p->roc_tab + tab.size());
-    CG_TRY(check_cuda(p, upload_roc(p, tab), "upload roll-off table"));
+    CG_TRY(check_cuda(p, plan_malloc(&p->roc_tab, sizeof(double) * tab.size()), "cudaMalloc roll-off table"));
+    CG_TRY(check_cuda(p, cudaMemcpy(p->roc_tab, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice),
+                      "upload roll-off table"));
   }
   if (lend_grid) {
     p->g = lend_grid;
@@ -514,7 +501,6 @@ void plan_release(Plan* p) {
   p->g = nullptr;
   cudaFree(p->roc_tab);
   p->roc_tab = nullptr;
-  p->roc_tab32 = nullptr;
   if (p->own_fft && p->fft) cufftDestroy(p->fft);
   p->fft = 0;
   for (int i = 0; i < 8; ++i)

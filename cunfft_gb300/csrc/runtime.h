@@ -34,9 +34,7 @@ struct Plan {
   cufftHandle fft_bwd_ext = 0;
   void* g = nullptr;           // batch * ntot complex
   bool own_g = false;
-  double* roc_tab = nullptr;   // per-dim roll-off factors 1 / phi_hat_t(k_t / n_t), sum_t N_t doubles,
-                               // followed in the same allocation by the same factors rounded to FP32
-  float* roc_tab32 = nullptr;  // that FP32 copy (the FP32 form's factors)
+  double* roc_tab = nullptr;   // per-dim roll-off factors 1 / phi_hat_t(k_t / n_t), sum_t N_t doubles
   Tiling tl{};
   Bins bins{};
   int64_t bins_capacity_M = -1;

@@ -1,8 +1,8 @@
 """Python front end of the extension API (include/cunfft_x.h) for torch CUDA tensors.
 
 ``NFFT`` wraps one cunfft_x plan: d-variate NFFT (d = 1..3, Gaussian or ES window) in
-FP64 (the reference's form) or FP32 (FP32 gridding, FFT and roll-off, FP64 node
-reduction), for ``batch`` instances with uneven node
+FP64 (the reference's form) or FP32 (FP32 gridding and FFT, FP64 node
+reduction and roll-off factors), for ``batch`` instances with uneven node
 counts.  Tensors stay on the device; calls run on the plan's CUDA stream, which
 defaults to torch's current stream so they order with surrounding torch work.
 

@@ -24,8 +24,8 @@
 extern "C" {
 #endif
 
-/** Precision of the gridding, FFT and roll-off stages.  FP64 is the reference's
- *  form; FP32 keeps FP64 only for the node-to-grid reduction. */
+/** Precision of the gridding and FFT stages.  FP64 is the reference's form;
+ *  FP32 keeps FP64 only for the node-to-grid reduction and the roll-off factors. */
 enum { CUNFFT_X_F64 = 0, CUNFFT_X_F32 = 1 };
 
 /** Spreading (adjoint gridding) kernel.  AUTO picks TENSOR where it applies
