@@ -205,11 +205,12 @@ __global__ void __launch_bounds__(kT2Threads, 1) k_spread2_tm(const float2* __re
       const unsigned char* sl = smem + L.rec_off + r * kT2SlotBytes;
       const uint32_t* offs = reinterpret_cast<const uint32_t*>(sl + kT2SlotOff);
       const float2* frs = reinterpret_cast<const float2*>(sl + kT2SlotFrac);
-      // Does any node of the batch reach this warp's rows (A: p0 in [32 lw, 32 lw + 32)) or
-      // columns (B: p1 in [16 b, 16 b + 16), b = lw - 4)?  Node j reaches [o_j, o_j + W).  With the
-      // binning's 16 x 16 sub-tile order a batch's window starts lie within a few rows and
-      // columns, so most operand warps of a batch only write zeros; the test is
-      // warp-uniform, and a warp that is reached computes exactly what it did before.
+      // Does any node of the batch reach this warp's rows (A: p0 in [32 lw, 32 lw + 32))
+      // or columns (B: p1 in [16 b, 16 b + 16), b = lw - 4)?  Node j reaches
+      // [o_j, o_j + W).  With the binning's 16 x 16 sub-tile order a batch's window starts
+      // lie within a few rows and columns, so most operand warps of a batch write zeros
+      // without evaluating taps (every tap of such a warp is zero, so for finite samples
+      // the operands are the same).  The test is warp-uniform.
       bool reached;
       {
         const uint32_t mo = offs[lane & (kTcK - 1)];
